@@ -1,0 +1,358 @@
+#!/usr/bin/env python
+"""Seconds per q-point of PyGW's polarization path — weights → χ0 → ε⁻¹ — on GB300.
+
+One step = one q-point of the workload: tetrahedron weights w_nm(k,q,iω), the
+χ0 contraction over all k, the symmetrised dielectric matrix and its inverse
+per frequency.  ``value`` is measured with every input already resident in
+HBM; ``e2e`` runs the same step through the package's public Python API from
+pinned host buffers (matrix elements streamed host→device per k-chunk) and
+reads ε⁻¹−1 back to the host.  Inputs are seeded synthetic data with the
+workload's shapes (no public dataset is involved).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload C2] [--impl gb300|reference]
+
+With N > 1 (torchrun) every rank is an independent replica over its own q
+points (the reference splits q over MPI ranks with no collective on this path);
+the timed region is bracketed by barriers and the maximum over ranks is kept.
+``--impl reference`` times the reference's CPU implementation of the path
+(the oracle's restatement: C++/OpenMP weights + numpy contraction and
+inverse) on the host cores, rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="C2")
+    ap.add_argument("--precision", default="fp64", choices=["fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload_desc(w):
+    return (f"{w.name}: {w.div}^3 k-mesh ({6 * w.div ** 3} tetrahedra), {w.nbands} bands ({w.nocc} occ), "
+            f"N_PB={w.npb}, {w.nom} log-spaced iw in {w.om_lo}-{w.om_hi} eV, {w.nq} q")
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            import tempfile
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------- problem
+class Inputs:
+    """Host and device inputs of one workload (matrix elements of one q reused)."""
+
+    def __init__(self, w, rank, device_resident=True):
+        import torch
+
+        from pygw_gb300 import synthetic as syn
+        self.w = w
+        self.p = syn.Problem(w)
+        b = self.p.bands
+        self.nomx, self.numin = b.nomax_numin
+        self.nb1, self.nb2 = b.nb1, b.nb2
+        self.P = self.nb1 * self.nb2
+        self.nkp = self.p.kqm.nkp
+        self.enk = b.enk()
+        self.ef = b.EF
+        self.omega = self.p.fr.omega
+        self.tetc = self.p.kqm.tetc
+        self.kqid = self.p.kqm.kqid
+        self.qs = self.p.qs
+        iq0 = self.qs[0]
+        sqv = syn.coulomb_sqrt(w, iq0, w.npb)
+        self.minm_host = torch.empty((self.nkp, self.P, w.npb), dtype=torch.complex128).pin_memory()
+        for ik in range(self.nkp):
+            m = syn.minm_k(w, b, self.p.kqm, iq0, ik, sqv).reshape(self.P, w.npb)
+            self.minm_host[ik].copy_(torch.from_numpy(m))
+        self.minm_dev = self.minm_host.cuda() if device_resident else None
+        self.enk_d = torch.from_numpy(np.ascontiguousarray(self.enk.T)).cuda()
+        self.tetc_d = torch.from_numpy(np.ascontiguousarray(self.tetc.T.astype(np.int32))).cuda()
+        self.kqid_d = torch.from_numpy(np.ascontiguousarray(self.kqid.T.astype(np.int32))).cuda()   # [iq][ik]
+        self.om_d = torch.from_numpy(self.omega.copy()).cuda()
+
+
+def gpu_step(inp, step, timers=None, stream=None):
+    """One q-point with device-resident inputs."""
+    from pygw_gb300 import eps as peps
+    from pygw_gb300 import polarization as pol
+    iq = inp.qs[step % len(inp.qs)]
+    r = pol.weights_device(inp.enk_d, inp.ef, inp.kqid_d[iq], 0, inp.nomx, inp.numin, inp.om_d, inp.tetc_d,
+                           stream=stream)
+    eps, _ = peps.chi0_accumulate(r.kcw, inp.minm_dev, inp.nkp, inp.w.npb, inp.nb1, inp.nb2, inp.w.nom,
+                                  stream=stream, timers=timers)
+    peps.chi0_finalize(eps, inp.w.npb, inp.w.nom, stream=stream)
+    return peps.eps_inverse(eps, inp.w.npb, inp.w.nom, stream=stream)
+
+
+def e2e_step(inp, step, out_host):
+    """One q-point through the public API from pinned host buffers; result read back."""
+    from pygw_gb300 import eps as peps
+    from pygw_gb300 import polarization as pol
+    iq = inp.qs[step % len(inp.qs)]
+    r = pol.weights_device(inp.enk, inp.ef, inp.kqid[:, iq], 0, inp.nomx, inp.numin, inp.omega, inp.tetc)
+    res = peps.chi0_eps(r, inp.minm_host, inp.nkp, inp.w.npb, inp.nb1, inp.nb2, inp.w.nom)
+    out_host.copy_(res.eps, non_blocking=True)
+    return res
+
+
+def fp64_peak_tflops():
+    """cuBLAS DGEMM throughput on this GPU (best of 3, 4096³)."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = 0.0
+    for _ in range(3):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        torch.cuda.synchronize()
+        best = max(best, 2.0 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    return best
+
+
+# ---------------------------------------------------------- CPU baseline
+def cpu_sample_seconds_per_q(w, nk_sample=8, threads=0):
+    """The reference's CPU path restated (oracle): full weights for one q, the
+    contraction timed on ``nk_sample`` k-points and scaled to all k, and the
+    inverse for every frequency.  Returns (seconds per q, description)."""
+    from oracle import weights as ow
+    from pygw_gb300 import synthetic as syn
+    p = syn.Problem(w)
+    b = p.bands
+    nomx, numin = b.nomax_numin
+    iq = p.qs[0]
+    t0 = time.perf_counter()
+    kcw = ow.bz_calcqdepw_par2(b.enk(), b.EF, p.kqm.kqid[:, iq], 0, nomx, numin, p.fr.omega, p.kqm.tetc,
+                               nthreads=threads)
+    t_w = time.perf_counter() - t0
+    sqv = syn.coulomb_sqrt(w, iq, w.npb)
+    nkp = p.kqm.nkp
+    nb1, nb2 = kcw.shape[:2]
+    ks = list(range(min(nk_sample, nkp)))
+    mins = [syn.minm_k(w, b, p.kqm, iq, ik, sqv) for ik in ks]
+    eps = np.zeros((w.npb, w.npb, w.nom), dtype=complex, order="F")
+    t0 = time.perf_counter()
+    for j, ik in enumerate(ks):                  # pygw.py:3170-3185
+        minm2 = np.reshape(mins[j], (nb1 * nb2, w.npb))
+        cminm2 = np.conj(minm2)
+        minm2Tc = minm2.T * -2.0
+        for iom in range(w.nom):
+            tmat = minm2Tc * kcw[:, :, ik, iom].ravel()
+            eps[:, :, iom] += np.matmul(tmat, cminm2)
+    t_c = (time.perf_counter() - t0) * nkp / len(ks)
+    import scipy.linalg
+    t0 = time.perf_counter()
+    Id = np.identity(w.npb)
+    for iom in range(w.nom):                     # pygw.py:3231-3268
+        e = (eps[:, :, iom] + np.conj(eps[:, :, iom].T)) / 2.0 + Id
+        eps[:, :, iom] = scipy.linalg.inv(e) - Id
+    t_i = time.perf_counter() - t0
+    desc = (f"oracle C++ weights for one q (all {nkp} k, {os.cpu_count()} threads) {t_w:.2f}s + numpy contraction "
+            f"timed on {len(ks)}/{nkp} k and scaled x{nkp / len(ks):.0f} ({t_c:.2f}s) + numpy inverse of all "
+            f"{w.nom} frequencies {t_i:.2f}s")
+    return t_w + t_c + t_i, desc
+
+
+def run_reference(a, w, rank):
+    if rank != 0:
+        return
+    from oracle.build import build as build_oracle
+    build_oracle()
+    cpu_sample_seconds_per_q(w, nk_sample=2)      # warm caches/threads (outside timing)
+    times, desc = [], ""
+    for i in range(a.warmup + a.steps):
+        t, desc = cpu_sample_seconds_per_q(w)
+        if i >= a.warmup:
+            times.append(t)
+    v = max(times)
+    line = {"metric": "s/q-point for chi0+eps^-1 (weights -> chi0 -> eps^-1)", "value": v, "unit": "s/q-point",
+            "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": v * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": workload_desc(w), "precision": "fp64", "parallelism": "replicas"},
+            "cpu_baseline": {"value": v, "unit": "s/q-point", "cores": os.cpu_count(), "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": v, "unit": "s/q-point", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# -------------------------------------------------------------------- main
+def main():
+    a = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    from pygw_gb300.synthetic import WORKLOADS
+    w = WORKLOADS[a.workload]
+    if a.impl == "reference":
+        return run_reference(a, w, rank)
+
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__
+    __graft_entry__.build()
+    from pygw_gb300 import _lib
+
+    lib = _lib.load()
+    inp = Inputs(w, rank)
+    # replicas: rank r visits q points r, r+world, ... (the reference's q split)
+    inp.qs = inp.qs[rank::world] or inp.qs[:1]
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    stream = torch.cuda.current_stream()
+    for s in range(a.warmup):
+        gpu_step(inp, s)
+    barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    timers = []
+    l0 = lib.pg_launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    ev0.record(stream)
+    for s in range(a.steps):
+        gpu_step(inp, a.warmup + s, timers=timers)
+    ev1.record(stream)
+    barrier()
+    launches = lib.pg_launch_count() - l0
+    clocks = sampler.stop()
+    dt = ev0.elapsed_time(ev1) * 1e-3
+    if dist is not None:
+        t = torch.tensor([dt], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dt = float(t.item())
+    value = dt / (a.steps * world)               # seconds per q-point, whole job
+    # dominant kernel: the χ0 contraction (one launch per step here)
+    chi0_ms = [s_.elapsed_time(e_) for s_, e_ in timers]
+    nb1, nb2, npb, nom = inp.nb1, inp.nb2, w.npb, w.nom
+    flops = 8.0 * npb * npb * nb1 * nb2 * inp.nkp * nom     # full complex GEMM count (reference's ZGEMMs)
+    achieved = flops / (statistics.mean(chi0_ms) * 1e-3) / 1e12
+    peak = fp64_peak_tflops()
+
+    e2e = None
+    if not a.no_e2e:
+        out_host = torch.empty((nom, npb, npb), dtype=torch.complex128).pin_memory()
+        for s in range(min(a.warmup, 1)):
+            e2e_step(inp, s, out_host)
+        barrier()
+        t0 = time.perf_counter()
+        for s in range(a.steps):
+            e2e_step(inp, s, out_host)
+        torch.cuda.synchronize()
+        et = time.perf_counter() - t0
+        if dist is not None:
+            t = torch.tensor([et], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            et = float(t.item())
+        h2d = (inp.minm_host.numel() * 16 + inp.enk.nbytes + inp.tetc.nbytes // 2 + inp.nkp * 4
+               + inp.omega.nbytes)
+        e2e = {"value": et / (a.steps * world), "unit": "s/q-point", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(out_host.numel() * 16)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        from oracle.build import build as build_oracle
+        build_oracle()
+        v, desc = cpu_sample_seconds_per_q(w)
+        cpu = {"value": v, "unit": "s/q-point", "cores": os.cpu_count(), "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {"metric": "s/q-point for chi0+eps^-1 (weights -> chi0 -> eps^-1)", "value": value,
+                "unit": "s/q-point", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+                "ms_per_step": dt / a.steps * 1e3, "higher_is_better": False, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": workload_desc(w), "precision": a.precision, "parallelism": "replicas",
+                           "l2": "inputs larger than L2 (matrix elements %.2f GB read every step)"
+                                 % (inp.minm_host.numel() * 16 / 1e9)},
+                "roofline": {"kernel": "k_chi0_f64", "bound": "fp64", "achieved": achieved, "peak": peak,
+                             "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                             "note": "algorithmic flops = 8*N_PB^2*P*Nk*Nw (full complex GEMM count) per launch; "
+                                     "peak = cuBLAS DGEMM measured in this run (no FP64 tensor path on GB300)"},
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,82 @@
+/* pygw_gb300 — C-ABI of the GB300 (sm_103a) polarization path.
+ *
+ * Plain pointers and sizes only.  Every array argument is a DEVICE pointer
+ * (allocated by the caller, e.g. as a torch CUDA tensor) unless stated
+ * otherwise; `stream` is a cudaStream_t (NULL = legacy default stream).
+ * Calls are stream-ordered and asynchronous: they enqueue kernels and return.
+ * Return value: PG_OK (0) or a negative PG_E* code (pygw_gb300/csrc/pygw_status.h).
+ * No entry point allocates memory; scratch space is passed in as `work`,
+ * sized by the matching *_workspace() query.
+ *
+ * Layouts follow the reference's arrays (Fortran order where the reference
+ * uses Fortran-ordered numpy arrays):
+ *   enk  [nbnd, nkp]              float64, enk[b + nbnd*k]
+ *   tetc [4, ntet]                int32, 0-based k indices
+ *   kqid [nkp]                    int32, 0-based (column iq of KQmesh.kqid)
+ *   kcw  [nb1, nb2, nkp, nom]     float64, nb1 = ncg+nomx+1, nb2 = nbnd-ncg-numin
+ *   minm [nk_chunk][P][N]         complex128 (interleaved re, im), P = nb1*nb2,
+ *                                 p = ie1*nb2 + ie2 — the per-k `minm2` blocks
+ *   eps  [N, N, nom]              complex128, eps[I + N*J + N*N*w]
+ *   epsw1, epsw2 [nom][N]         complex128; head [nom] complex128
+ */
+#ifndef PYGW_GB300_H
+#define PYGW_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ weights
+ * Replaces the f2py call
+ *     kcw = ft.bz_calcqdepw_par2(enk, ef, kqid, ncg, nomx, numin, omega, tetc)
+ * made by Polarization_weights (pygw.py:3443), i.e. the Fortran subroutine
+ * bz_calcqdepw_par2 (for_tetrahedra.f90:390-464) with its callees
+ * (for_tetrahedra3.f90:3-743, for_tetrahedra2.f90:1688-2773).
+ * Requires ntet == 6*nkp (tetrahedron 6*ik+t links to 6*kqid[ik]+t,
+ * for_tetrahedra.f90:426-432).  kcw is fully overwritten.
+ * nom_chunk > 0 bounds the scratch: frequencies are processed in chunks of
+ * that size (0 = all at once).  d_status (device, 1 uint, may be NULL)
+ * receives PG_ERR_* bits OR-ed in; d_counters (device, PG_NCOUNTERS uint64,
+ * may be NULL) receives PG_CNT_* counts added in.  The reference stops the
+ * process on the PG_ERR_* conditions; here the affected (tetrahedron, band
+ * pair) contributes zero and the bit is set. */
+size_t pg_bz_calcqdepw_par2_workspace(int nbnd, int nkp, int ncg, int nomx, int numin, int nom, int ntet,
+                                      int nom_chunk);
+int pg_bz_calcqdepw_par2(const double* enk, int nbnd, int nkp, double ef, const int* kqid, int ncg, int nomx,
+                         int numin, const double* omega, int nom, const int* tetc, int ntet, double* kcw, void* work,
+                         size_t work_bytes, int nom_chunk, unsigned* d_status, unsigned long long* d_counters,
+                         void* stream);
+
+/* --------------------------------------------------------- χ0, plain FP64
+ * Replaces the k loop of MatrixElements2Band.calc_eps (pygw.py:3083-3200):
+ *     eps[:, :, w] += (minm2ᵀ·coef ⊙ kcw[:, :, k, w].ravel()) @ conj(minm2)
+ *     epsw1[:, w]  += (minm2ᵀ·coef ⊙ kcw[:, :, k, w].ravel()) @ pm       (q = 0)
+ * for the k-points k0 .. k0+nk_chunk-1 whose minm blocks are passed.
+ * Accumulates into eps/epsw1 (caller zeroes them before the first chunk).
+ * Only tiles on or above the diagonal are accumulated; call
+ * pg_chi0_mirror_f64 once after the last chunk to fill the rest.
+ * coef = -fspin = -2 in the reference.  pm/epsw1 both NULL for q != 0. */
+int pg_chi0_accumulate_f64(const void* minm, int nk_chunk, int k0, const double* kcw, int nb1, int nb2, int nkp,
+                           int nom, int npb, double coef, void* eps, const void* pm, void* epsw1, void* stream);
+int pg_chi0_mirror_f64(void* eps, int npb, int nom, void* stream);
+
+/* ----------------------------------------------------- ε and ε⁻¹, FP64
+ * Replaces pygw.py:3229-3271: symmetrise, +1, invert (scipy.linalg.inv),
+ * q = 0 head/wings update, -1.  On return eps holds ε⁻¹ − 1; epsw1, epsw2,
+ * head are updated in place when epsw1 != NULL (q = 0). */
+size_t pg_eps_inverse_f64_workspace(int npb, int nom);
+int pg_eps_inverse_f64(void* eps, int npb, int nom, void* epsw1, void* epsw2, void* head, void* work,
+                       size_t work_bytes, void* stream);
+
+/* ------------------------------------------------------------ bookkeeping
+ * Number of kernels this library has enqueued since it was loaded (all entry
+ * points, all streams).  No counterpart in the reference. */
+unsigned long long pg_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYGW_GB300_H */

