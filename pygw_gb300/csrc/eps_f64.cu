@@ -78,9 +78,9 @@ __global__ void k_gj_pivot(double2* eps, int N, int k, int* perm) {
     }
     __syncthreads();
   }
-  const int p = si[0];
+  const int p = (si[0] < N) ? si[0] : k;   // a column without a finite pivot keeps its row
   if (threadIdx.x == 0) perm[(size_t)N * w + k] = p;
-  if (p != k && p < N) {
+  if (p != k) {
     for (int j = threadIdx.x; j < N; j += blockDim.x) {
       const double2 t = E[(size_t)k + (size_t)N * j];
       E[(size_t)k + (size_t)N * j] = E[(size_t)p + (size_t)N * j];
@@ -128,7 +128,7 @@ __global__ void k_gj_unpermute(double2* eps, int N, const int* perm) {
   double2* E = eps + (size_t)N * N * w;
   for (int k = N - 1; k >= 0; k--) {
     const int p = perm[(size_t)N * w + k];
-    if (p != k) {
+    if (p != k && p >= 0 && p < N) {
       for (int i = threadIdx.x; i < N; i += blockDim.x) {
         const double2 t = E[(size_t)i + (size_t)N * k];
         E[(size_t)i + (size_t)N * k] = E[(size_t)i + (size_t)N * p];
