@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--div", type=int, default=0, help="override the k-mesh divisions (smaller profiling case)")
+    ap.add_argument("--npb", type=int, default=0, help="override the product-basis size (smaller profiling case)")
     return ap.parse_args()
 
 
@@ -56,7 +58,13 @@ def workload_desc(w):
 
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi sampling of SM clocks and throttle reasons.
+
+    The sampler process is started before this process initialises CUDA (no
+    fork of a process that holds a CUDA context) and runs for the whole
+    bench; ``window(t0, t1)`` summarises the samples taken inside a timed
+    region (host wall-clock times)."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -77,32 +85,43 @@ class ClockSampler:
             self.proc = None
 
     def stop(self):
-        if self.proc is None:
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def window(self, t0, t1):
+        if self.path is None or not os.path.exists(self.path):
             return None
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except Exception:
-            self.proc.kill()
+        import datetime
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.path):
             parts = [x.strip() for x in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                clk, mx = float(parts[2]), float(parts[3])
             except ValueError:
                 continue
-            for n, v in zip(names, parts[5:9]):
+            if not (t0 - 0.25 <= ts <= t1 + 0.25):
+                continue
+            sm.append(clk)
+            smax.append(mx)
+            for n, v in zip(names, parts[6:10]):
                 if v.lower().startswith("active"):
                     reasons.add(n)
-        os.unlink(self.path)
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+    def cleanup(self):
+        if self.path and os.path.exists(self.path):
+            os.unlink(self.path)
 
 
 # --------------------------------------------------------------- problem
@@ -253,20 +272,26 @@ def main():
     a = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    from pygw_gb300.synthetic import WORKLOADS
+    from pygw_gb300.synthetic import WORKLOADS, scaled
     w = WORKLOADS[a.workload]
+    if a.div or a.npb:
+        w = scaled(w, div=a.div or w.div, npb=a.npb or w.npb)
     if a.impl == "reference":
         return run_reference(a, w, rank)
 
-    import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    sampler = ClockSampler(local)
+    sampler.start()                    # before CUDA is initialised in this process
+    import __graft_entry__
+    __graft_entry__.build()            # any compiler subprocess also runs before CUDA init
+    from oracle.build import build as build_oracle
+    build_oracle()
+    import torch
     torch.cuda.set_device(local)
     dist = None
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    import __graft_entry__
-    __graft_entry__.build()
     from pygw_gb300 import _lib
 
     lib = _lib.load()
@@ -283,19 +308,18 @@ def main():
     for s in range(a.warmup):
         gpu_step(inp, s)
     barrier()
-    sampler = ClockSampler(local)
-    sampler.start()
     timers = []
     l0 = lib.pg_launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
+    wall0 = time.time()
     ev0.record(stream)
     for s in range(a.steps):
         gpu_step(inp, a.warmup + s, timers=timers)
     ev1.record(stream)
     barrier()
+    wall1 = time.time()
     launches = lib.pg_launch_count() - l0
-    clocks = sampler.stop()
     dt = ev0.elapsed_time(ev1) * 1e-3
     if dist is not None:
         t = torch.tensor([dt], device="cuda")
@@ -331,11 +355,13 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
-        from oracle.build import build as build_oracle
-        build_oracle()
         v, desc = cpu_sample_seconds_per_q(w)
         cpu = {"value": v, "unit": "s/q-point", "cores": os.cpu_count(), "kind": "port", "sample": desc}
 
+    torch.cuda.synchronize()
+    sampler.stop()
+    clocks = sampler.window(wall0, wall1)
+    sampler.cleanup()
     if rank == 0:
         line = {"metric": "s/q-point for chi0+eps^-1 (weights -> chi0 -> eps^-1)", "value": value,
                 "unit": "s/q-point", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
