@@ -126,7 +126,11 @@ class ClockSampler:
 
 # --------------------------------------------------------------- problem
 class Inputs:
-    """Host and device inputs of one workload (matrix elements of one q reused)."""
+    """Host and device inputs of one workload (matrix elements of one q reused).
+
+    Every host buffer the e2e path copies from, and the buffer it reads the
+    result into, is pinned here once, before any GPU work; the timed loops
+    issue no pageable copies."""
 
     def __init__(self, w, rank, device_resident=True):
         import torch
@@ -151,11 +155,19 @@ class Inputs:
         for ik in range(self.nkp):
             m = syn.minm_k(w, b, self.p.kqm, iq0, ik, sqv).reshape(self.P, w.npb)
             self.minm_host[ik].copy_(torch.from_numpy(m))
+        # pinned host copies in the C-ABI layouts
+        self.enk_h = torch.from_numpy(np.ascontiguousarray(self.enk.T)).pin_memory()                # [nkp][nbnd]
+        self.tetc_h = torch.from_numpy(np.ascontiguousarray(self.tetc.T.astype(np.int32))).pin_memory()
+        self.kqid_h = torch.from_numpy(np.ascontiguousarray(self.kqid.T.astype(np.int32))).pin_memory()  # [iq][ik]
+        self.om_h = torch.from_numpy(self.omega.copy()).pin_memory()
+        self.out_h = torch.empty((w.nom, w.npb, w.npb), dtype=torch.complex128).pin_memory()
+        torch.cuda.synchronize()
         self.minm_dev = self.minm_host.cuda() if device_resident else None
-        self.enk_d = torch.from_numpy(np.ascontiguousarray(self.enk.T)).cuda()
-        self.tetc_d = torch.from_numpy(np.ascontiguousarray(self.tetc.T.astype(np.int32))).cuda()
-        self.kqid_d = torch.from_numpy(np.ascontiguousarray(self.kqid.T.astype(np.int32))).cuda()   # [iq][ik]
-        self.om_d = torch.from_numpy(self.omega.copy()).cuda()
+        self.enk_d = self.enk_h.cuda()
+        self.tetc_d = self.tetc_h.cuda()
+        self.kqid_d = self.kqid_h.cuda()
+        self.om_d = self.om_h.cuda()
+        torch.cuda.synchronize()
 
 
 def gpu_step(inp, step, timers=None, stream=None):
@@ -176,7 +188,7 @@ def e2e_step(inp, step, out_host):
     from pygw_gb300 import eps as peps
     from pygw_gb300 import polarization as pol
     iq = inp.qs[step % len(inp.qs)]
-    r = pol.weights_device(inp.enk, inp.ef, inp.kqid[:, iq], 0, inp.nomx, inp.numin, inp.omega, inp.tetc)
+    r = pol.weights_device(inp.enk_h, inp.ef, inp.kqid_h[iq], 0, inp.nomx, inp.numin, inp.om_h, inp.tetc_h)
     res = peps.chi0_eps(r, inp.minm_host, inp.nkp, inp.w.npb, inp.nb1, inp.nb2, inp.w.nom)
     out_host.copy_(res.eps, non_blocking=True)
     return res
@@ -335,7 +347,7 @@ def main():
 
     e2e = None
     if not a.no_e2e:
-        out_host = torch.empty((nom, npb, npb), dtype=torch.complex128).pin_memory()
+        out_host = inp.out_h
         for s in range(min(a.warmup, 1)):
             e2e_step(inp, s, out_host)
         barrier()

@@ -52,8 +52,9 @@ def weights_device(enk, ef, kqid, ncg, nomx, numin, omega, tetc, nom_chunk=0, st
     """Compute ``kcw`` on the GPU; arguments as in ``bz_calcqdepw_par2``.
 
     ``enk`` [nbnd, nkp] and ``tetc`` [4, ntet] may be numpy (any order) or
-    CUDA tensors already laid out as the C-ABI expects (enk as [nkp][nbnd],
-    tetc as [ntet][4]).
+    tensors already laid out as the C-ABI expects (enk as [nkp][nbnd], tetc as
+    [ntet][4]); CPU tensors (pinned for asynchronous copies) are copied to the
+    device on the current stream.
     """
     require_cuda()
     lib = _lib.load()
@@ -62,13 +63,13 @@ def weights_device(enk, ef, kqid, ncg, nomx, numin, omega, tetc, nom_chunk=0, st
         enk_d = to_device(np.asarray(enk, dtype=np.float64).T, torch.float64)   # [nkp][nbnd]
     else:
         nkp, nbnd = enk.shape
-        enk_d = enk
+        enk_d = to_device(enk, torch.float64)
     if isinstance(tetc, np.ndarray):
         ntet = tetc.shape[1]
         tetc_d = to_device(np.asarray(tetc, dtype=np.int32).T, torch.int32)    # [ntet][4]
     else:
         ntet = tetc.shape[0]
-        tetc_d = tetc
+        tetc_d = to_device(tetc, torch.int32)
     kqid_d = to_device(np.asarray(kqid, dtype=np.int32) if isinstance(kqid, np.ndarray) else kqid, torch.int32)
     om_d = to_device(np.asarray(omega, dtype=np.float64) if isinstance(omega, np.ndarray) else omega, torch.float64)
     nom = int(om_d.shape[0])
