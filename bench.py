@@ -194,23 +194,10 @@ def e2e_step(inp, step, out_host):
     return res
 
 
-def fp64_peak_tflops():
-    """cuBLAS DGEMM throughput on this GPU (best of 3, 4096³)."""
-    import torch
-    n = 4096
-    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    torch.matmul(a, b)
-    best = 0.0
-    for _ in range(3):
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        s.record()
-        torch.matmul(a, b)
-        e.record()
-        torch.cuda.synchronize()
-        best = max(best, 2.0 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
-    return best
+# GB300's FP64 rate (CUDA cores; it has no faster FP64 tensor path).  The
+# measured peaks file holds HBM and bf16 figures only, so the FP64
+# roofline of the plain path is quoted against this nominal figure.
+FP64_NOMINAL_TFLOPS = 1.25
 
 
 # ---------------------------------------------------------- CPU baseline
@@ -343,7 +330,7 @@ def main():
     nb1, nb2, npb, nom = inp.nb1, inp.nb2, w.npb, w.nom
     flops = 8.0 * npb * npb * nb1 * nb2 * inp.nkp * nom     # full complex GEMM count (reference's ZGEMMs)
     achieved = flops / (statistics.mean(chi0_ms) * 1e-3) / 1e12
-    peak = fp64_peak_tflops()
+    peak = FP64_NOMINAL_TFLOPS
 
     e2e = None
     if not a.no_e2e:
@@ -385,7 +372,7 @@ def main():
                 "roofline": {"kernel": "k_chi0_f64", "bound": "fp64", "achieved": achieved, "peak": peak,
                              "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
                              "note": "algorithmic flops = 8*N_PB^2*P*Nk*Nw (full complex GEMM count) per launch; "
-                                     "peak = cuBLAS DGEMM measured in this run (no FP64 tensor path on GB300)"},
+                                     "peak = nominal GB300 FP64 (no measured FP64 figure available)"},
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks}
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -109,6 +109,13 @@ def chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=None, k_chunk=Non
         m = minm.reshape(nkp, P, npb)
         bufs = [torch.empty((k_chunk, P, npb), dtype=torch.complex128, device="cuda") for _ in range(2)]
         copy_stream = torch.cuda.Stream()
+        # The buffers come from the caching allocator of the compute stream and
+        # may reuse memory that kernels still queued there (e.g. the weight
+        # kernel's workspace) are using: the copy stream starts after them, and
+        # the allocator is told the buffers are also used on the copy stream.
+        copy_stream.wait_stream(cur)
+        for b in bufs:
+            b.record_stream(copy_stream)
         copied = [torch.cuda.Event() for _ in range(2)]
         used = [None, None]
         for i, k0 in enumerate(range(0, nkp, k_chunk)):
