@@ -81,3 +81,34 @@ def test_drop_in_calc_eps():
     ref = oe.calc_eps(kcw, lambda ik: minm[ik], w.npb)
     assert e1 is None and eps.shape == (w.npb, w.npb, kcw.shape[-1])
     assert _rel(eps, ref[0]) < TOL
+
+
+def test_chi0_input_paths_agree():
+    """Per-k callable, device-resident tensor and pinned host tensor (streamed
+    in double-buffered k-chunks on a side stream) give the same χ0."""
+    w, p, kcw, minm = _problem()
+    nb1, nb2, nkp, nom = kcw.shape
+    P = nb1 * nb2
+    kd = peps._kcw_device(kcw)
+    a, _ = peps.chi0_accumulate(kd, lambda ik: minm[ik], nkp, w.npb, nb1, nb2, nom, k_chunk=7)
+    host = torch.from_numpy(np.stack([m.reshape(P, w.npb) for m in minm])).pin_memory()
+    b, _ = peps.chi0_accumulate(kd, host.cuda(), nkp, w.npb, nb1, nb2, nom)
+    c, _ = peps.chi0_accumulate(kd, host, nkp, w.npb, nb1, nb2, nom, k_chunk=5)
+    torch.cuda.synchronize()
+    a, b, c = (x.cpu().numpy() for x in (a, b, c))
+    assert _rel(b, a) < 1e-13 and _rel(c, a) < 1e-13
+
+
+def test_weights_from_pinned_tensors_match_numpy_inputs():
+    from pygw_gb300 import polarization as pol
+    w, p, kcw, minm = _problem()
+    b = p.bands
+    nomx, numin = b.nomax_numin
+    iq = p.qs[0]
+    enk_h = torch.from_numpy(np.ascontiguousarray(b.enk().T)).pin_memory()
+    tetc_h = torch.from_numpy(np.ascontiguousarray(p.kqm.tetc.T.astype(np.int32))).pin_memory()
+    kq_h = torch.from_numpy(np.ascontiguousarray(p.kqm.kqid[:, iq].astype(np.int32))).pin_memory()
+    om_h = torch.from_numpy(p.fr.omega.copy()).pin_memory()
+    r = pol.weights_device(enk_h, b.EF, kq_h, 0, nomx, numin, om_h, tetc_h)
+    torch.cuda.synchronize()
+    assert np.array_equal(r.numpy(), kcw)
