@@ -39,7 +39,8 @@ extern "C" {
  * nom_chunk > 0 bounds the scratch: frequencies are processed in chunks of
  * that size (0 = all at once).  d_status (device, 1 uint, may be NULL)
  * receives PG_ERR_* bits OR-ed in; d_counters (device, PG_NCOUNTERS uint64,
- * may be NULL) receives PG_CNT_* counts added in.  The reference stops the
+ * may be NULL) receives PG_CNT_* counts added in (the per-polyhedron counts
+ * once per frequency chunk).  The reference stops the
  * process on the PG_ERR_* conditions; here the affected (tetrahedron, band
  * pair) contributes zero and the bit is set. */
 size_t pg_bz_calcqdepw_par2_workspace(int nbnd, int nkp, int ncg, int nomx, int numin, int nom, int ntet,
@@ -48,6 +49,22 @@ int pg_bz_calcqdepw_par2(const double* enk, int nbnd, int nkp, double ef, const 
                          int numin, const double* omega, int nom, const int* tetc, int ntet, double* kcw, void* work,
                          size_t work_bytes, int nom_chunk, unsigned* d_status, unsigned long long* d_counters,
                          void* stream);
+
+/* Same computation for callers that cannot allocate device memory (a Fortran
+ * or C host program reaching the library through a foreign-function layer
+ * with no device allocator, or a service held to a fixed memory budget).  No
+ * counterpart in the reference.  Takes no workspace: its scratch is a
+ * file-scope device array of pg_bz_calcqdepw_par2_noalloc_capacity() bytes
+ * (256 MiB) that each GPU using the library holds until the process exits;
+ * frequencies are processed in chunks that fit.  Returns PG_ETOOBIG when the
+ * k lists plus one frequency of scratch (4*ntet*nb1*nb2 doubles) do not fit.
+ * All calls share that array: calls that overlap on the GPU race and must be
+ * serialised.  The first call on a device looks up the array's device address
+ * and caches it; make that call before any stream capture. */
+size_t pg_bz_calcqdepw_par2_noalloc_capacity(void);
+int pg_bz_calcqdepw_par2_noalloc(const double* enk, int nbnd, int nkp, double ef, const int* kqid, int ncg,
+                                 int nomx, int numin, const double* omega, int nom, const int* tetc, int ntet,
+                                 double* kcw, unsigned* d_status, unsigned long long* d_counters, void* stream);
 
 /* --------------------------------------------------------- χ0, plain FP64
  * Replaces the k loop of MatrixElements2Band.calc_eps (pygw.py:3083-3200):

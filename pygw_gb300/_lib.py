@@ -20,6 +20,10 @@ SIGNATURES = {
     "pg_bz_calcqdepw_par2": (c_int, [c_void_p, c_int, c_int, c_double, c_void_p, c_int, c_int, c_int, c_void_p,
                                      c_int, c_void_p, c_int, c_void_p, c_void_p, c_size_t, c_int, c_void_p,
                                      c_void_p, c_void_p]),
+    "pg_bz_calcqdepw_par2_noalloc_capacity": (c_size_t, []),
+    "pg_bz_calcqdepw_par2_noalloc": (c_int, [c_void_p, c_int, c_int, c_double, c_void_p, c_int, c_int, c_int,
+                                             c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
+                                             c_void_p]),
     "pg_chi0_accumulate_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_int, c_int, c_int,
                                        c_double, c_void_p, c_void_p, c_void_p, c_void_p]),
     "pg_chi0_mirror_f64": (c_int, [c_void_p, c_int, c_int, c_void_p]),

@@ -30,3 +30,6 @@
 #define PG_CNT_BIGW_WARN 18        // |w| > 1e4 at ω ≥ 1e-6 (reference prints a warning)
 #define PG_CNT_BIGW_ZEROED 19      // |w| > 1e4 at ω < 1e-6 (reference zeroes it)
 #define PG_NCOUNTERS 20
+
+// Size of the device array used by pg_bz_calcqdepw_par2_noalloc (256 MiB).
+#define PG_NOALLOC_SCRATCH_BYTES (256ull << 20)

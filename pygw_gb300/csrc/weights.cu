@@ -1112,3 +1112,66 @@ extern "C" int pg_bz_calcqdepw_par2(const double* enk, int nbnd, int nkp, double
   cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? PG_OK : PG_ECUDA;
 }
+
+// ---------------------------------------------------------------------------
+// Weights without any device allocation by the caller.
+//
+// Some callers cannot allocate device memory: host code that reaches this
+// library through a thin foreign-function layer (a Fortran program over
+// ISO_C_BINDING, an f2py wrapper) has no device allocator of its own, and
+// services that run under a fixed device-memory budget may not allocate per
+// call.  pg_bz_calcqdepw_par2_noalloc takes only the inputs and the output
+// kcw; its scratch (the k → tetrahedron lists and the per-tetrahedron weights
+// of one frequency chunk) lives in a file-scope device array of
+// PG_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
+// the process exits.  Frequencies are processed in chunks that fit; a problem
+// whose k lists plus ONE frequency of scratch exceed the array is rejected
+// with PG_ETOOBIG.  The array keeps the previous call's contents; nothing in
+// it has to start at zero, because every call rewrites each entry it reads.
+// All calls share the one array, so calls whose work overlaps on the GPU
+// (different streams, or other threads) race: serialise them.
+// The first call on a device looks up the array's device address (with that
+// device current) and caches it; make that first call before any stream
+// capture.
+namespace pgw {
+static __device__ __align__(256) unsigned char g_noalloc_scratch[PG_NOALLOC_SCRATCH_BYTES];
+}
+
+#include <mutex>
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_ptr[64] = {nullptr};
+
+extern "C" size_t pg_bz_calcqdepw_par2_noalloc_capacity(void) { return (size_t)PG_NOALLOC_SCRATCH_BYTES; }
+
+extern "C" int pg_bz_calcqdepw_par2_noalloc(const double* enk, int nbnd, int nkp, double ef, const int* kqid,
+                                            int ncg, int nomx, int numin, const double* omega, int nom,
+                                            const int* tetc, int ntet, double* kcw, unsigned* d_status,
+                                            unsigned long long* d_counters, void* stream) {
+  const int nb1 = ncg + nomx + 1, nb2 = nbnd - ncg - numin;
+  if (!enk || !kqid || !omega || !tetc || !kcw) return PG_EARG;
+  if (nb1 <= 0 || nb2 <= 0 || nkp <= 0 || ntet <= 0 || nom <= 0 || ncg < 0 || numin < 0) return PG_EARG;
+  if (ntet != 6 * nkp) return PG_EARG;
+  // Largest frequency chunk whose scratch fits next to the k lists.
+  const size_t lists = align256(sizeof(int) * (size_t)(nkp + 1)) + align256(sizeof(int) * (size_t)nkp) +
+                       align256(sizeof(int) * (size_t)4 * ntet);
+  const size_t per_omega = sizeof(double) * (size_t)4 * ntet * (size_t)nb1 * nb2;
+  if (lists + per_omega + 256 > (size_t)PG_NOALLOC_SCRATCH_BYTES) return PG_ETOOBIG;
+  const size_t fit = ((size_t)PG_NOALLOC_SCRATCH_BYTES - lists - 256) / per_omega;
+  const int nomc = (int)((fit < (size_t)nom) ? fit : (size_t)nom);
+  // One-time per-device lookup of the array's device address: in host code
+  // the symbol names a host-side stand-in, not device memory.
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return PG_ECUDA;
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, pgw::g_noalloc_scratch) != cudaSuccess || !p) return PG_ECUDA;
+      g_noalloc_ptr[dev] = p;
+    }
+    base = g_noalloc_ptr[dev];
+  }
+  return pg_bz_calcqdepw_par2(enk, nbnd, nkp, ef, kqid, ncg, nomx, numin, omega, nom, tetc, ntet, kcw, base,
+                              (size_t)PG_NOALLOC_SCRATCH_BYTES, nomc, d_status, d_counters, stream);
+}
