@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="C2")
-    ap.add_argument("--precision", default="fp64", choices=["fp64"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--div", type=int, default=0, help="override the k-mesh divisions (smaller profiling case)")
@@ -170,26 +170,32 @@ class Inputs:
         torch.cuda.synchronize()
 
 
-def gpu_step(inp, step, timers=None, stream=None):
+def gpu_step(inp, step, timers=None, stream=None, precision="fp64"):
     """One q-point with device-resident inputs."""
     from pygw_gb300 import eps as peps
     from pygw_gb300 import polarization as pol
     iq = inp.qs[step % len(inp.qs)]
     r = pol.weights_device(inp.enk_d, inp.ef, inp.kqid_d[iq], 0, inp.nomx, inp.numin, inp.om_d, inp.tetc_d,
                            stream=stream)
-    eps, _ = peps.chi0_accumulate(r.kcw, inp.minm_dev, inp.nkp, inp.w.npb, inp.nb1, inp.nb2, inp.w.nom,
-                                  stream=stream, timers=timers)
-    peps.chi0_finalize(eps, inp.w.npb, inp.w.nom, stream=stream)
+    if precision == "mixed":
+        eps, status, inp.mwork = peps.chi0_mixed(r.kcw, inp.minm_dev, inp.nkp, inp.w.npb, inp.nb1, inp.nb2,
+                                                 inp.w.nom, omega_batch=inp.wb, stream=stream,
+                                                 work=getattr(inp, "mwork", None), timers=timers)
+        inp.statuses.append(status)
+    else:
+        eps, _ = peps.chi0_accumulate(r.kcw, inp.minm_dev, inp.nkp, inp.w.npb, inp.nb1, inp.nb2, inp.w.nom,
+                                      stream=stream, timers=timers)
+        peps.chi0_finalize(eps, inp.w.npb, inp.w.nom, stream=stream)
     return peps.eps_inverse(eps, inp.w.npb, inp.w.nom, stream=stream)
 
 
-def e2e_step(inp, step, out_host):
+def e2e_step(inp, step, out_host, precision="fp64"):
     """One q-point through the public API from pinned host buffers; result read back."""
     from pygw_gb300 import eps as peps
     from pygw_gb300 import polarization as pol
     iq = inp.qs[step % len(inp.qs)]
     r = pol.weights_device(inp.enk_h, inp.ef, inp.kqid_h[iq], 0, inp.nomx, inp.numin, inp.om_h, inp.tetc_h)
-    res = peps.chi0_eps(r, inp.minm_host, inp.nkp, inp.w.npb, inp.nb1, inp.nb2, inp.w.nom)
+    res = peps.chi0_eps(r, inp.minm_host, inp.nkp, inp.w.npb, inp.nb1, inp.nb2, inp.w.nom, precision=precision)
     out_host.copy_(res.eps, non_blocking=True)
     return res
 
@@ -295,6 +301,10 @@ def main():
 
     lib = _lib.load()
     inp = Inputs(w, rank)
+    inp.statuses = []
+    if a.precision == "mixed":
+        from pygw_gb300 import eps as peps
+        inp.wb = peps.mixed_omega_batch(inp.nb1, inp.nb2, inp.nkp, w.npb, w.nom)
     # replicas: rank r visits q points r, r+world, ... (the reference's q split)
     inp.qs = inp.qs[rank::world] or inp.qs[:1]
 
@@ -305,7 +315,7 @@ def main():
 
     stream = torch.cuda.current_stream()
     for s in range(a.warmup):
-        gpu_step(inp, s)
+        gpu_step(inp, s, precision=a.precision)
     barrier()
     timers = []
     l0 = lib.pg_launch_count()
@@ -314,7 +324,7 @@ def main():
     wall0 = time.time()
     ev0.record(stream)
     for s in range(a.steps):
-        gpu_step(inp, a.warmup + s, timers=timers)
+        gpu_step(inp, a.warmup + s, timers=timers, precision=a.precision)
     ev1.record(stream)
     barrier()
     wall1 = time.time()
@@ -325,22 +335,44 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         dt = float(t.item())
     value = dt / (a.steps * world)               # seconds per q-point, whole job
-    # dominant kernel: the χ0 contraction (one launch per step here)
+    # dominant kernel: the χ0 contraction (one launch sequence per step)
     chi0_ms = [s_.elapsed_time(e_) for s_, e_ in timers]
     nb1, nb2, npb, nom = inp.nb1, inp.nb2, w.npb, w.nom
     flops = 8.0 * npb * npb * nb1 * nb2 * inp.nkp * nom     # full complex GEMM count (reference's ZGEMMs)
     achieved = flops / (statistics.mean(chi0_ms) * 1e-3) / 1e12
-    peak = FP64_NOMINAL_TFLOPS
+    status_bits = 0
+    for st in inp.statuses:
+        status_bits |= int(st.item())
+    if a.precision == "mixed":
+        peaks = json.load(open(PEAKS_FILE)) if os.path.exists(PEAKS_FILE) else {}
+        peak = peaks.get("bf16_tflops", 1900.0)
+        peak_note = "of measured" if "bf16_tflops" in peaks else "of fallback"
+        rpad = ((2 * npb + 127) // 128) * 128
+        ntile = rpad // 128
+        kpad = ((inp.nkp * nb1 * nb2 + 63) // 64) * 64
+        executed = 15 * 2.0 * 128 * 128 * kpad * (ntile * (ntile + 1) // 2) * nom
+        roof = {"kernel": "k_ozaki_gemm (+ digit kernels, assembly)", "bound": "tensor", "achieved": achieved,
+                "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "executed_bf16_tflops": executed / (statistics.mean(chi0_ms) * 1e-3) / 1e12,
+                "note": "achieved = 8*N_PB^2*P*Nk*Nw (the reference's full complex-GEMM flops) / chi0 time; "
+                        "executed_bf16 = 15 digit-pair products on the upper-triangle 128x128 tiles; peak = bf16 "
+                        + peak_note}
+    else:
+        peak = FP64_NOMINAL_TFLOPS
+        roof = {"kernel": "k_chi0_f64", "bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
+                "note": "algorithmic flops = 8*N_PB^2*P*Nk*Nw (full complex GEMM count) per launch; "
+                        "peak = nominal GB300 FP64 (no measured FP64 figure available)"}
 
     e2e = None
     if not a.no_e2e:
         out_host = inp.out_h
         for s in range(min(a.warmup, 1)):
-            e2e_step(inp, s, out_host)
+            e2e_step(inp, s, out_host, a.precision)
         barrier()
         t0 = time.perf_counter()
         for s in range(a.steps):
-            e2e_step(inp, s, out_host)
+            e2e_step(inp, s, out_host, a.precision)
         torch.cuda.synchronize()
         et = time.perf_counter() - t0
         if dist is not None:
@@ -365,14 +397,12 @@ def main():
         line = {"metric": "s/q-point for chi0+eps^-1 (weights -> chi0 -> eps^-1)", "value": value,
                 "unit": "s/q-point", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
                 "ms_per_step": dt / a.steps * 1e3, "higher_is_better": False, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "vs_baseline": None, "dtype": "f64" if a.precision == "fp64" else "bf16-digits/f32-exact/f64",
+                "data": "synthetic",
                 "config": {"workload": workload_desc(w), "precision": a.precision, "parallelism": "replicas",
                            "l2": "inputs larger than L2 (matrix elements %.2f GB read every step)"
                                  % (inp.minm_host.numel() * 16 / 1e9)},
-                "roofline": {"kernel": "k_chi0_f64", "bound": "fp64", "achieved": achieved, "peak": peak,
-                             "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
-                             "note": "algorithmic flops = 8*N_PB^2*P*Nk*Nw (full complex GEMM count) per launch; "
-                                     "peak = nominal GB300 FP64 (no measured FP64 figure available)"},
+                "roofline": roof, "kernel_status": status_bits,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks}
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -78,6 +78,29 @@ int pg_bz_calcqdepw_par2_noalloc(const double* enk, int nbnd, int nkp, double ef
 int pg_chi0_accumulate_f64(const void* minm, int nk_chunk, int k0, const double* kcw, int nb1, int nb2, int nkp,
                            int nom, int npb, double coef, void* eps, const void* pm, void* epsw1, void* stream);
 int pg_chi0_mirror_f64(void* eps, int npb, int nom, void* stream);
+/* The q→0 wings alone (epsw1 += tmat @ pm, pygw.py:3192-3195), for use with
+ * the split-precision χ0 below. */
+int pg_wings_f64(const void* minm, int nk_chunk, int k0, const double* kcw, int nb1, int nb2, int nkp, int nom,
+                 int npb, double coef, const void* pm, void* epsw1, void* stream);
+
+/* ------------------------------------------------- χ0, split precision
+ * Same sum as pg_chi0_accumulate_f64 over ALL k at once (minm holds every
+ * k: [nkp][P][N]), on the tensor cores: the matrix elements and the weighted
+ * matrix elements are split into five 8-bit digits per value with one
+ * exponent per row, digit products are summed exactly (tcgen05 MMA into
+ * FP32 tensor memory, renormalised every 896 K-values), and only digit pairs
+ * below 2^-40 are dropped.  Writes the full Hermitian χ0 to eps (no mirror
+ * needed).  omega_batch frequencies share one set of weighted digits
+ * (workspace grows with it); kb_split > 0 caps the K-blocks per CTA
+ * (0 = automatic).  d_status receives PG_ERR_TIMEOUT if a pipeline wait
+ * expired (the result is then invalid). */
+size_t pg_chi0_mixed_workspace(int nb1, int nb2, int nkp, int npb, int omega_batch, int kb_split);
+int pg_chi0_mixed(const void* minm, int nkp, const double* kcw, int nb1, int nb2, int nom, int npb, double coef,
+                  void* eps, void* work, size_t work_bytes, int omega_batch, int kb_split, unsigned* d_status,
+                  void* stream);
+/* Workspace layout (byte offsets and sizes) for inspection by tests. */
+int pg_chi0_mixed_layout(int nb1, int nb2, int nkp, int npb, int omega_batch, int kb_split, size_t* offs,
+                         long long* dims);
 
 /* ----------------------------------------------------- ε and ε⁻¹, FP64
  * Replaces pygw.py:3229-3271: symmetrise, +1, invert (scipy.linalg.inv),

@@ -25,6 +25,7 @@ SOURCES = {
     "chi0_f64.cu": [],
     "eps_f64.cu": [],
     "launches.cu": [],
+    "chi0_mixed.cu": [],
 }
 
 

@@ -176,3 +176,16 @@ extern "C" int pg_chi0_mirror_f64(void* eps, int npb, int nom, void* stream) {
   pg_count_launches(1);
   return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ECUDA;
 }
+
+// q→0 wings only (the mixed-precision path computes χ0 itself).
+extern "C" int pg_wings_f64(const void* minm, int nk_chunk, int k0, const double* kcw, int nb1, int nb2, int nkp,
+                            int nom, int npb, double coef, const void* pm, void* epsw1, void* stream) {
+  if (!minm || !kcw || !pm || !epsw1 || nk_chunk <= 0 || k0 < 0 || k0 + nk_chunk > nkp || nb1 <= 0 || nb2 <= 0 ||
+      nom <= 0 || npb <= 0)
+    return PG_EARG;
+  dim3 g2((npb + 127) / 128, nom);
+  k_wings_f64<<<g2, 128, 0, (cudaStream_t)stream>>>((const double2*)minm, nk_chunk, k0, kcw, nb1, nb2, nkp, npb, coef,
+                                                    (const double2*)pm, (double2*)epsw1);
+  pg_count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ECUDA;
+}

@@ -18,6 +18,7 @@
 #define PG_ERR_EQUIV (1u << 4)      // stweight_imag_par bad equiv_flag (for_tetrahedra3.f90:687-690)
 #define PG_ERR_UNDEFINED (1u << 5)  // reference reads uninitialised data / writes through index 0
 #define PG_ERR_NONFINITE (1u << 6)  // a non-finite weight was produced
+#define PG_ERR_TIMEOUT (1u << 7)    // a bounded wait inside a pipelined kernel expired
 
 // Counters (unsigned long long) accumulated by the weight kernel; the same
 // layout as the oracle's statistics.

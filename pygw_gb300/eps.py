@@ -19,7 +19,7 @@ import torch
 from . import _lib
 from .device import ptr, require_cuda, stream_handle, to_device, workspace
 
-PRECISION = "fp64"      # 'fp64' (plain comparator) or 'mixed'
+PRECISION = "fp64"      # 'fp64' (plain comparator) or 'mixed' (split-precision tensor-core χ0)
 FSPIN = 2.0
 
 
@@ -149,6 +149,72 @@ def chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=None, k_chunk=Non
     return eps, epsw1
 
 
+def _all_k_device(minm, nkp, P, npb):
+    """Matrix elements of every k as one CUDA tensor [nkp, P, npb] (complex128)."""
+    if isinstance(minm, torch.Tensor):
+        m = minm.reshape(nkp, P, npb)
+        return m if m.is_cuda else m.cuda(non_blocking=True)
+    out = torch.empty((nkp, P, npb), dtype=torch.complex128, device="cuda")
+    for ik in range(nkp):
+        mm = minm(ik)
+        t = mm if isinstance(mm, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(mm, dtype=np.complex128))
+        out[ik].copy_(t.reshape(P, npb))
+    return out
+
+
+def mixed_omega_batch(nb1, nb2, nkp, npb, nom, budget_bytes=None):
+    """Frequencies per batch of the split-precision χ0, sized to a memory budget
+    (default: 40 % of the free device memory)."""
+    lib = _lib.load()
+    if budget_bytes is None:
+        free, _ = torch.cuda.mem_get_info()
+        budget_bytes = int(0.4 * free)
+    wb = 1
+    while wb < nom and lib.pg_chi0_mixed_workspace(nb1, nb2, nkp, npb, 2 * wb, 0) <= budget_bytes:
+        wb *= 2
+    return min(wb, nom)
+
+
+def chi0_mixed(kcw_d, minm, nkp, npb, nb1, nb2, nom, omega_batch=None, kb_split=0, stream=None, work=None,
+               timers=None):
+    """Split-precision χ0 (tensor cores) for all frequencies: returns
+    ``(eps, status, work)`` with the full Hermitian χ0 in ``eps`` [nom][N][N]."""
+    lib = _lib.load()
+    P = nb1 * nb2
+    m = _all_k_device(minm, nkp, P, npb)
+    wb = omega_batch or mixed_omega_batch(nb1, nb2, nkp, npb, nom)
+    wbytes = lib.pg_chi0_mixed_workspace(nb1, nb2, nkp, npb, wb, int(kb_split))
+    if work is None or work.numel() < wbytes:
+        work = workspace(wbytes)
+    eps = torch.empty((nom, npb, npb), dtype=torch.complex128, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    s = torch.cuda.current_stream() if stream is None else stream
+    ev = None
+    if timers is not None:
+        ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        ev[0].record(s)
+    rc = lib.pg_chi0_mixed(ptr(m), nkp, ptr(kcw_d), nb1, nb2, nom, npb, -FSPIN, ptr(eps), ptr(work), work.numel(),
+                           int(wb), int(kb_split), ptr(status), stream_handle(stream))
+    _lib.check(rc, "pg_chi0_mixed")
+    if ev is not None:
+        ev[1].record(s)
+        timers.append(ev)
+    return eps, status, work
+
+
+def wings_f64(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k, stream=None):
+    """q→0 wings ``epsw1[ω][I]`` in FP64 (pygw.py:3192-3195)."""
+    lib = _lib.load()
+    P = nb1 * nb2
+    m = _all_k_device(minm, nkp, P, npb)
+    pmd = to_device(np.stack([np.asarray(pm_k(ik), dtype=np.complex128) for ik in range(nkp)]), torch.complex128)
+    epsw1 = torch.zeros((nom, npb), dtype=torch.complex128, device="cuda")
+    rc = lib.pg_wings_f64(ptr(m), nkp, 0, ptr(kcw_d), nb1, nb2, nkp, nom, npb, -FSPIN, ptr(pmd), ptr(epsw1),
+                          stream_handle(stream))
+    _lib.check(rc, "pg_wings_f64")
+    return epsw1
+
+
 def chi0_finalize(eps, npb, nom, stream=None, precision=None):
     lib = _lib.load()
     rc = lib.pg_chi0_mirror_f64(ptr(eps), npb, nom, stream_handle(stream))
@@ -180,6 +246,13 @@ def chi0_eps(kcw, minm, nkp, npb, nb1, nb2, nom, pm_k=None, head=None, k_chunk=N
     ``minm``: per-k callable or ``[nkp, P, npb]`` tensor (see chi0_accumulate)."""
     require_cuda()
     kcw_d = _kcw_device(kcw)
+    precision = precision or PRECISION
+    if precision == "mixed":
+        eps, status, _ = chi0_mixed(kcw_d, minm, nkp, npb, nb1, nb2, nom, stream=stream, timers=timers)
+        epsw1 = wings_f64(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k, stream=stream) if pm_k is not None else None
+        r = eps_inverse(eps, npb, nom, epsw1=epsw1, head=head, stream=stream)
+        r.status = status
+        return r
     eps, epsw1 = chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=pm_k, k_chunk=k_chunk, stream=stream,
                                  precision=precision, timers=timers)
     chi0_finalize(eps, npb, nom, stream=stream, precision=precision)

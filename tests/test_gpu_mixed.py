@@ -1,0 +1,141 @@
+"""Split-precision χ0 on the tensor cores (sm_103a, through the C-ABI).
+
+1. White box: the digits the GPU produced are read back from its workspace,
+   every digit-group integer I_d = Σ_{s+t=d} Σ_K a_s b_t is recomputed
+   exactly in numpy (float64 sums of small integers below 2^53), and the
+   kernel's output tiles must match bit for bit — this checks the TMA
+   layout, the MMA descriptors, the exactness of the FP32 tensor-core
+   accumulation of integer products and the renormalisation between chunks.
+2. The digits represent their values to the expected 2^-40 (row scale).
+3. End to end: χ0 within 1e-10 of the FP64 oracle at each row/column scale
+   (|Δχ0_IJ| ≤ tol·sqrt(|χ0_II χ0_JJ|)) and ε⁻¹ within 1e-9 (max relative).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import eps as oe
+from oracle import weights as ow
+from pygw_gb300 import _lib
+from pygw_gb300 import eps as peps
+from pygw_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+S = 5
+
+
+def _problem(w):
+    p = syn.Problem(w)
+    b = p.bands
+    nomx, numin = b.nomax_numin
+    iq = p.qs[0]
+    kcw = ow.bz_calcqdepw_par2(b.enk(), b.EF, p.kqm.kqid[:, iq], 0, nomx, numin, p.fr.omega, p.kqm.tetc)
+    sqv = syn.coulomb_sqrt(w, iq, w.npb)
+    minm = [syn.minm_k(w, b, p.kqm, iq, ik, sqv) for ik in range(p.kqm.nkp)]
+    return p, kcw, minm
+
+
+def _bf16(u16):
+    return (u16.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+
+
+def test_digit_gemm_is_exact_white_box():
+    w = syn.scaled(syn.WORKLOADS["C1"], div=3, npb=100, nom=3)
+    p, kcw, minm = _problem(w)
+    nb1, nb2, nkp, nom = kcw.shape
+    P, N = nb1 * nb2, w.npb
+    lib = _lib.load()
+    kd = peps._kcw_device(kcw)
+    wb, kb_split = 2, 100
+    eps, status, work = peps.chi0_mixed(kd, lambda ik: minm[ik], nkp, N, nb1, nb2, nom, omega_batch=wb,
+                                        kb_split=kb_split)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    offs = (ctypes.c_size_t * 9)()
+    dims = (ctypes.c_longlong * 9)()
+    assert lib.pg_chi0_mixed_layout(nb1, nb2, nkp, N, wb, kb_split, offs, dims) == 0
+    K, K_pad, R, R_pad, nT, npair, nkb, nsplit, kbs = list(dims)
+    assert nsplit == 3 and nT == 2
+    raw = work.cpu().numpy()
+
+    def view(i, dtype, shape):
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        return raw[offs[i]:offs[i] + n].view(dtype).reshape(shape)
+
+    A = _bf16(view(0, np.uint16, (S, R_pad, K_pad)))
+    B = _bf16(view(1, np.uint16, (wb, S, R_pad, K_pad)))[0]     # last batch: frequency nom-1 in slot 0
+    eA = view(5, np.int32, (R_pad,))
+    fB = view(6, np.int32, (wb, R_pad))[0]
+    out = view(7, np.float64, (nsplit, wb, npair, 128, 128))[:, 0]
+    assert np.abs(A).max() <= 129 and np.abs(B).max() <= 129
+
+    # (2) digits represent V and c·w·V
+    M = np.concatenate([m.reshape(P, N) for m in minm])                    # [K, N]
+    V = np.zeros((R_pad, K_pad))
+    V[:N, :K] = M.real.T
+    V[N:2 * N, :K] = M.imag.T
+    scal = 2.0 ** -(8.0 * (np.arange(S) + 1))
+    Vrec = np.einsum("srk,s->rk", A, scal) * 2.0 ** eA[:, None]
+    assert np.all(np.abs(Vrec - V) <= 2.0 ** (eA[:, None] - 40.0))
+    cw = -2.0 * np.array([kcw[:, :, ik, nom - 1].ravel() for ik in range(nkp)]).ravel()
+    cw = np.concatenate([cw, np.zeros(K_pad - K)])
+    Brec = np.einsum("srk,s->rk", B, scal) * 2.0 ** fB[:, None]
+    assert np.all(np.abs(Brec - Vrec * cw[None, :]) <= 2.0 ** (fB[:, None] - 38.0))
+
+    # (1) exact group integers, combined in the kernel's order
+    pair = 0
+    for ti in range(nT):
+        for tj in range(ti, nT):
+            ra, rb = slice(128 * ti, 128 * ti + 128), slice(128 * tj, 128 * tj + 128)
+            for sp in range(nsplit):
+                ks = slice(sp * kbs * 64, min(K_pad, (sp + 1) * kbs * 64))
+                acc = None
+                for d in range(S):
+                    I = sum(A[s, ra, ks] @ B[d - s, rb, ks].T for s in range(d + 1))
+                    v = I * 2.0 ** (-8 * d)
+                    acc = v if acc is None else acc + v
+                got = out[sp, pair].T            # stored [col][row]
+                assert np.array_equal(got, acc), (ti, tj, sp, np.abs(got - acc).max())
+            pair += 1
+
+
+def _row_scaled_err(a, ref):
+    d = np.sqrt(np.abs(np.einsum("iiw->iw", ref)))
+    return np.max(np.abs(a - ref) / (d[:, None, :] * d[None, :, :] + 1e-300))
+
+
+@pytest.mark.parametrize("name,kw", [("C1", {}), ("C2", {"div": 4})])
+def test_mixed_chi0_and_inverse_accuracy(name, kw):
+    w = syn.scaled(syn.WORKLOADS[name], **kw) if kw else syn.WORKLOADS[name]
+    p, kcw, minm = _problem(w)
+    nb1, nb2, nkp, nom = kcw.shape
+    ref = oe.calc_eps(kcw, lambda ik: minm[ik], w.npb)
+    chi0_ref = ref[4]
+    chi0_ref = (chi0_ref + np.conj(chi0_ref.transpose(1, 0, 2))) / 2
+    kd = peps._kcw_device(kcw)
+    eps, status, _ = peps.chi0_mixed(kd, lambda ik: minm[ik], nkp, w.npb, nb1, nb2, nom)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    chi0 = eps.cpu().numpy().transpose(2, 1, 0)
+    assert _row_scaled_err(chi0, chi0_ref) < 1e-10
+    r = peps.chi0_eps(kcw, lambda ik: minm[ik], nkp, w.npb, nb1, nb2, nom, precision="mixed")
+    einv = r.numpy()[0] + np.eye(w.npb)[:, :, None]
+    einv_ref = ref[0] + np.eye(w.npb)[:, :, None]
+    rel = max(np.max(np.abs(einv[..., o] - einv_ref[..., o])) / np.max(np.abs(einv_ref[..., o])) for o in range(nom))
+    assert rel < 1e-9, rel
+
+
+def test_mixed_q0_wings_and_head():
+    w = syn.scaled(syn.WORKLOADS["C1"], div=3, npb=96, nom=6)
+    p, kcw, minm = _problem(w)
+    nb1, nb2, nkp, nom = kcw.shape
+    pms = [syn.pm_k(w, p.bands, ik) for ik in range(nkp)]
+    head0 = syn.head_from_weights(kcw, pms)
+    ref = oe.calc_eps(kcw, lambda ik: minm[ik], w.npb, pm_k=lambda ik: pms[ik], head=head0)
+    r = peps.chi0_eps(kcw, lambda ik: minm[ik], nkp, w.npb, nb1, nb2, nom, pm_k=lambda ik: pms[ik], head=head0,
+                      precision="mixed")
+    eps, w1, w2, head = r.numpy()
+    assert np.max(np.abs(head - ref[3])) / np.max(np.abs(ref[3])) < 1e-9
+    assert np.max(np.abs(w1 - ref[1])) / np.max(np.abs(ref[1])) < 1e-9
