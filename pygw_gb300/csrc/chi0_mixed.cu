@@ -425,12 +425,11 @@ __global__ void k_digits_A(const double2* __restrict__ minm, long long K, int N,
   }
 }
 
-// Weights for a batch of frequencies: c·w as an FP32 pair, and per K-block max |c·w|.
+// Weights for a batch of frequencies: c·w as an FP32 pair (hi + lo ≈ 48 bits).
 __global__ void k_weights_prep(const double* __restrict__ kcw, int nb1, int nb2, int nkp, int om0, int wb, double coef,
-                               long long K, long long K_pad, float2* wpair, float* wblk, int nkb) {
+                               long long K, long long K_pad, float2* wpair) {
   const int kb = blockIdx.x, wl = blockIdx.y;
   const int P = nb1 * nb2;
-  float m = 0.0f;
   for (int j = threadIdx.x; j < KB; j += blockDim.x) {
     const long long k = (long long)kb * KB + j;
     float2 pr = make_float2(0.0f, 0.0f);
@@ -441,35 +440,43 @@ __global__ void k_weights_prep(const double* __restrict__ kcw, int nb1, int nb2,
       const float hi = __double2float_rn(w);
       const float lo = __double2float_rn(w - (double)hi);
       pr = make_float2(hi, lo);
-      m = fmaxf(m, __double2float_ru(fabs(w)));
     }
     wpair[(size_t)wl * K_pad + k] = pr;
   }
-  __shared__ float sm[64];
-  sm[threadIdx.x] = m;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) sm[threadIdx.x] = fmaxf(sm[threadIdx.x], sm[threadIdx.x + s]);
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) wblk[(size_t)wl * nkb + kb] = sm[0];
 }
 
-__global__ void k_row_exp_B(const float* tmax, const float* wblk, const int* eA, int R, int R_pad, int nkb, int* fB) {
-  const int r = blockIdx.x, wl = blockIdx.y;
+// Exact row maxima of |V_trunc·c·w| per frequency (V relative to 2^eA), as
+// float bits: nonnegative floats order like unsigned integers.
+__global__ void k_rowmax_B(const __nv_bfloat16* __restrict__ adig, const float2* __restrict__ wpair, int R, int R_pad,
+                           long long K_pad, unsigned* rmax) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y, wl = blockIdx.z;
   float m = 0.0f;
-  if (r < R)
-    for (int kb = threadIdx.x; kb < nkb; kb += blockDim.x)
-      m = fmaxf(m, __fmul_ru(tmax[(size_t)r * nkb + kb], wblk[(size_t)wl * nkb + kb]));
-  __shared__ float sm[256];
-  sm[threadIdx.x] = m;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) sm[threadIdx.x] = fmaxf(sm[threadIdx.x], sm[threadIdx.x + s]);
-    __syncthreads();
+  if (k < K_pad && r < R) {
+    const float a0 = __bfloat162float(adig[((size_t)0 * R_pad + r) * K_pad + k]);
+    const float a1 = __bfloat162float(adig[((size_t)1 * R_pad + r) * K_pad + k]);
+    const float a2 = __bfloat162float(adig[((size_t)2 * R_pad + r) * K_pad + k]);
+    const float vhi = (a0 * 0x1p-8f + a1 * 0x1p-16f) + a2 * 0x1p-24f;
+    m = __fmul_ru(fabsf(vhi), fabsf(wpair[(size_t)wl * K_pad + k].x));
   }
-  // |V_trunc| may exceed |V| by 2^(eA−41): covered by the 1+1e-6 margin in row_exponent
-  if (threadIdx.x == 0) fB[(size_t)wl * R_pad + r] = row_exponent(sm[0]);
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ float sm[8];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float mm = sm[0];
+    for (int i = 1; i < (int)(blockDim.x >> 5); i++) mm = fmaxf(mm, sm[i]);
+    if (mm > 0.0f) atomicMax(rmax + (size_t)wl * R_pad + r, __float_as_uint(mm));
+  }
+}
+
+// fB = eA + exponent of the row maximum (with margin for the low-order terms
+// of the product, which row_exponent's 1+1e-6 factor covers).
+__global__ void k_row_exp_B(const unsigned* rmax, const int* eA, int R, int R_pad, int nw, int* fB) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nw * R_pad) return;
+  const int r = i % R_pad;
+  fB[i] = (r < R) ? eA[r] + row_exponent(__uint_as_float(rmax[i])) : 0;
 }
 
 // B digits of c·w_K·V[r,K] from the A digits, in FP32 pair arithmetic:
@@ -540,7 +547,7 @@ static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 struct MixedLayout {
   long long K, K_pad;
   int N, R, R_pad, nT, npair, nkb, nsplit, kb_per_split, wb;
-  size_t off_adig, off_bdig, off_tmax, off_wpair, off_wblk, off_eA, off_fB, off_out, total;
+  size_t off_adig, off_bdig, off_tmax, off_wpair, off_rmax, off_eA, off_fB, off_out, total;
 };
 
 static MixedLayout mixed_layout(int nb1, int nb2, int nkp, int npb, int wb, int kb_split) {
@@ -564,7 +571,7 @@ static MixedLayout mixed_layout(int nb1, int nb2, int nkp, int npb, int wb, int 
   L.off_bdig = o; o += al256((size_t)wb * S * L.R_pad * L.K_pad * 2);
   L.off_tmax = o; o += al256((size_t)L.R_pad * L.nkb * 4);
   L.off_wpair = o; o += al256((size_t)wb * L.K_pad * 8);
-  L.off_wblk = o; o += al256((size_t)wb * L.nkb * 4);
+  L.off_rmax = o; o += al256((size_t)wb * L.R_pad * 4);     // row maxima of |V·c·w| (float bits)
   L.off_eA = o; o += al256((size_t)L.R_pad * 4);
   L.off_fB = o; o += al256((size_t)wb * L.R_pad * 4);
   L.off_out = o; o += al256((size_t)L.nsplit * wb * L.npair * TM * TM * 8);
@@ -622,7 +629,7 @@ extern "C" int pg_chi0_mixed(const void* minm, int nkp, const double* kcw, int n
   __nv_bfloat16* bdig = (__nv_bfloat16*)(w + L.off_bdig);
   float* tmax = (float*)(w + L.off_tmax);
   float2* wpair = (float2*)(w + L.off_wpair);
-  float* wblk = (float*)(w + L.off_wblk);
+  unsigned* rmax = (unsigned*)(w + L.off_rmax);
   int* eA = (int*)(w + L.off_eA);
   int* fB = (int*)(w + L.off_fB);
   double* out = (double*)(w + L.off_out);
@@ -649,27 +656,29 @@ extern "C" int pg_chi0_mixed(const void* minm, int nkp, const double* kcw, int n
   for (int om0 = 0; om0 < nom; om0 += wb) {
     const int nw = (om0 + wb <= nom) ? wb : nom - om0;
     op.wb = wb;
-    k_weights_prep<<<dim3(L.nkb, nw), 64, 0, s>>>(kcw, nb1, nb2, nkp, om0, nw, coef, L.K, L.K_pad, wpair, wblk,
-                                                  L.nkb);
-    k_row_exp_B<<<dim3(L.R_pad, nw), 256, 0, s>>>(tmax, wblk, eA, L.R, L.R_pad, L.nkb, fB);
+    k_weights_prep<<<dim3(L.nkb, nw), 64, 0, s>>>(kcw, nb1, nb2, nkp, om0, nw, coef, L.K, L.K_pad, wpair);
+    if (cudaMemsetAsync(rmax, 0, (size_t)L.wb * L.R_pad * 4, s) != cudaSuccess) return PG_ECUDA;
+    k_rowmax_B<<<dim3((unsigned)((L.K_pad + 255) / 256), L.R_pad, nw), 256, 0, s>>>(adig, wpair, L.R, L.R_pad,
+                                                                                   L.K_pad, rmax);
+    k_row_exp_B<<<(nw * L.R_pad + 255) / 256, 256, 0, s>>>(rmax, eA, L.R, L.R_pad, nw, fB);
     k_digits_B<<<dim3((unsigned)((L.K_pad + 255) / 256), L.R_pad, nw), 256, 0, s>>>(adig, eA, wpair, fB, L.R, L.R_pad,
                                                                                    L.K_pad, nw, bdig);
     k_ozaki_gemm<<<dim3(L.npair, nw, L.nsplit), NTHREADS, smem, s>>>(mapA, mapB, op);
     k_assemble<<<dim3((npb + 127) / 128, npb, nw), 128, 0, s>>>(out, eA, fB, npb, L.R_pad, L.nT, L.npair, L.nsplit,
                                                                wb, om0, (double2*)eps);
-    pg_count_launches(5);
+    pg_count_launches(6);
   }
   return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ECUDA;
 }
 
 // Workspace layout of pg_chi0_mixed, for inspection by tests:
-// offs = {adig, bdig, tmax, wpair, wblk, eA, fB, out, total} (bytes),
+// offs = {adig, bdig, tmax, wpair, rmax, eA, fB, out, total} (bytes),
 // dims = {K, K_pad, R, R_pad, nT, npair, nkb, nsplit, kb_per_split}.
 extern "C" int pg_chi0_mixed_layout(int nb1, int nb2, int nkp, int npb, int omega_batch, int kb_split, size_t* offs,
                                     long long* dims) {
   if (nb1 <= 0 || nb2 <= 0 || nkp <= 0 || npb <= 0 || omega_batch <= 0 || !offs || !dims) return PG_EARG;
   MixedLayout L = mixed_layout(nb1, nb2, nkp, npb, omega_batch, kb_split);
-  const size_t o[9] = {L.off_adig, L.off_bdig, L.off_tmax, L.off_wpair, L.off_wblk, L.off_eA, L.off_fB, L.off_out,
+  const size_t o[9] = {L.off_adig, L.off_bdig, L.off_tmax, L.off_wpair, L.off_rmax, L.off_eA, L.off_fB, L.off_out,
                        L.total};
   const long long d[9] = {L.K, L.K_pad, L.R, L.R_pad, L.nT, L.npair, L.nkb, L.nsplit, L.kb_per_split};
   for (int i = 0; i < 9; i++) { offs[i] = o[i]; dims[i] = d[i]; }

@@ -57,7 +57,7 @@ def test_digit_gemm_is_exact_white_box():
     dims = (ctypes.c_longlong * 9)()
     assert lib.pg_chi0_mixed_layout(nb1, nb2, nkp, N, wb, kb_split, offs, dims) == 0
     K, K_pad, R, R_pad, nT, npair, nkb, nsplit, kbs = list(dims)
-    assert nsplit == 3 and nT == 2
+    assert nsplit >= 2 and nT == 2
     raw = work.cpu().numpy()
 
     def view(i, dtype, shape):
