@@ -42,8 +42,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="C2")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default="C3")
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--fp64-k-sample", type=int, default=4,
+                    help="k-points on which the plain FP64 GPU contraction is timed for the comparison line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--div", type=int, default=0, help="override the k-mesh divisions (smaller profiling case)")
@@ -170,13 +172,21 @@ class Inputs:
         torch.cuda.synchronize()
 
 
-def gpu_step(inp, step, timers=None, stream=None, precision="fp64"):
-    """One q-point with device-resident inputs."""
+def gpu_step(inp, step, timers=None, stream=None, precision="fp64", phases=None):
+    """One q-point with device-resident inputs; ``phases`` (a list) receives
+    CUDA events bracketing weights / χ0 / ε⁻¹."""
+    import torch
     from pygw_gb300 import eps as peps
     from pygw_gb300 import polarization as pol
     iq = inp.qs[step % len(inp.qs)]
+    cs = torch.cuda.current_stream() if stream is None else stream
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)] if phases is not None else None
+    if ev:
+        ev[0].record(cs)
     r = pol.weights_device(inp.enk_d, inp.ef, inp.kqid_d[iq], 0, inp.nomx, inp.numin, inp.om_d, inp.tetc_d,
                            stream=stream)
+    if ev:
+        ev[1].record(cs)
     if precision == "mixed":
         eps, status, inp.mwork = peps.chi0_mixed(r.kcw, inp.minm_dev, inp.nkp, inp.w.npb, inp.nb1, inp.nb2,
                                                  inp.w.nom, omega_batch=inp.wb, stream=stream,
@@ -186,7 +196,45 @@ def gpu_step(inp, step, timers=None, stream=None, precision="fp64"):
         eps, _ = peps.chi0_accumulate(r.kcw, inp.minm_dev, inp.nkp, inp.w.npb, inp.nb1, inp.nb2, inp.w.nom,
                                       stream=stream, timers=timers)
         peps.chi0_finalize(eps, inp.w.npb, inp.w.nom, stream=stream)
-    return peps.eps_inverse(eps, inp.w.npb, inp.w.nom, stream=stream)
+    if ev:
+        ev[2].record(cs)
+    res = peps.eps_inverse(eps, inp.w.npb, inp.w.nom, stream=stream)
+    if ev:
+        ev[3].record(cs)
+        phases.append(ev)
+    return res
+
+
+def fp64_gpu_estimate(inp, nk):
+    """Seconds per q-point of the plain FP64 GPU path: weights and ε⁻¹ timed in
+    full, the FP64 contraction timed on ``nk`` k-points and scaled to all k."""
+    import torch
+    from pygw_gb300 import _lib
+    from pygw_gb300 import eps as peps
+    from pygw_gb300 import polarization as pol
+    from pygw_gb300.device import ptr, stream_handle
+    lib = _lib.load()
+    nk = max(1, min(nk, inp.nkp))
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    cs = torch.cuda.current_stream()
+    iq = inp.qs[0]
+    ev[0].record(cs)
+    r = pol.weights_device(inp.enk_d, inp.ef, inp.kqid_d[iq], 0, inp.nomx, inp.numin, inp.om_d, inp.tetc_d)
+    ev[1].record(cs)
+    eps = torch.zeros((inp.w.nom, inp.w.npb, inp.w.npb), dtype=torch.complex128, device="cuda")
+    rc = lib.pg_chi0_accumulate_f64(ptr(inp.minm_dev), nk, 0, ptr(r.kcw), inp.nb1, inp.nb2, inp.nkp, inp.w.nom,
+                                    inp.w.npb, -2.0, ptr(eps), None, None, stream_handle(None))
+    _lib.check(rc, "pg_chi0_accumulate_f64")
+    peps.chi0_finalize(eps, inp.w.npb, inp.w.nom)
+    ev[2].record(cs)
+    peps.eps_inverse(eps, inp.w.npb, inp.w.nom)
+    ev[3].record(cs)
+    torch.cuda.synchronize()
+    t_w = ev[0].elapsed_time(ev[1]) * 1e-3
+    t_c = ev[1].elapsed_time(ev[2]) * 1e-3 * inp.nkp / nk
+    t_i = ev[2].elapsed_time(ev[3]) * 1e-3
+    return t_w + t_c + t_i, {"weights_s": t_w, "chi0_s": t_c, "eps_inverse_s": t_i,
+                             "sample": f"FP64 contraction timed on {nk}/{inp.nkp} k-points and scaled"}
 
 
 def e2e_step(inp, step, out_host, precision="fp64"):
@@ -207,45 +255,49 @@ FP64_NOMINAL_TFLOPS = 1.25
 
 
 # ---------------------------------------------------------- CPU baseline
-def cpu_sample_seconds_per_q(w, nk_sample=8, threads=0):
-    """The reference's CPU path restated (oracle): full weights for one q, the
-    contraction timed on ``nk_sample`` k-points and scaled to all k, and the
-    inverse for every frequency.  Returns (seconds per q, description)."""
+def cpu_sample_seconds_per_q(w, nk_sample=2, nom_sample=8, threads=0):
+    """The reference's CPU path restated (oracle), timed on a bounded sample:
+    the weights for ``nom_sample`` of the frequencies (the work is linear in
+    them), the contraction for ``nk_sample`` k-points at every frequency, and
+    the inverse for ``nom_sample`` frequencies; each part is scaled to the full
+    q-point.  Returns (seconds per q, description)."""
     from oracle import weights as ow
     from pygw_gb300 import synthetic as syn
+    import scipy.linalg
     p = syn.Problem(w)
     b = p.bands
     nomx, numin = b.nomax_numin
     iq = p.qs[0]
+    om = p.fr.omega
+    osel = np.linspace(0, len(om) - 1, min(nom_sample, len(om))).round().astype(int)
     t0 = time.perf_counter()
-    kcw = ow.bz_calcqdepw_par2(b.enk(), b.EF, p.kqm.kqid[:, iq], 0, nomx, numin, p.fr.omega, p.kqm.tetc,
-                               nthreads=threads)
-    t_w = time.perf_counter() - t0
+    kcw_s = ow.bz_calcqdepw_par2(b.enk(), b.EF, p.kqm.kqid[:, iq], 0, nomx, numin, om[osel], p.kqm.tetc,
+                                 nthreads=threads)
+    t_w = (time.perf_counter() - t0) * len(om) / len(osel)
     sqv = syn.coulomb_sqrt(w, iq, w.npb)
     nkp = p.kqm.nkp
-    nb1, nb2 = kcw.shape[:2]
+    nb1, nb2 = kcw_s.shape[:2]
     ks = list(range(min(nk_sample, nkp)))
     mins = [syn.minm_k(w, b, p.kqm, iq, ik, sqv) for ik in ks]
-    eps = np.zeros((w.npb, w.npb, w.nom), dtype=complex, order="F")
+    eps = np.zeros((w.npb, w.npb, len(om)), dtype=complex, order="F")
     t0 = time.perf_counter()
     for j, ik in enumerate(ks):                  # pygw.py:3170-3185
         minm2 = np.reshape(mins[j], (nb1 * nb2, w.npb))
         cminm2 = np.conj(minm2)
         minm2Tc = minm2.T * -2.0
-        for iom in range(w.nom):
-            tmat = minm2Tc * kcw[:, :, ik, iom].ravel()
+        for iom in range(len(om)):
+            tmat = minm2Tc * kcw_s[:, :, ik, iom % len(osel)].ravel()
             eps[:, :, iom] += np.matmul(tmat, cminm2)
     t_c = (time.perf_counter() - t0) * nkp / len(ks)
-    import scipy.linalg
     t0 = time.perf_counter()
     Id = np.identity(w.npb)
-    for iom in range(w.nom):                     # pygw.py:3231-3268
+    for iom in osel:                             # pygw.py:3231-3268
         e = (eps[:, :, iom] + np.conj(eps[:, :, iom].T)) / 2.0 + Id
         eps[:, :, iom] = scipy.linalg.inv(e) - Id
-    t_i = time.perf_counter() - t0
-    desc = (f"oracle C++ weights for one q (all {nkp} k, {os.cpu_count()} threads) {t_w:.2f}s + numpy contraction "
-            f"timed on {len(ks)}/{nkp} k and scaled x{nkp / len(ks):.0f} ({t_c:.2f}s) + numpy inverse of all "
-            f"{w.nom} frequencies {t_i:.2f}s")
+    t_i = (time.perf_counter() - t0) * len(om) / len(osel)
+    desc = (f"oracle C++ weights on {len(osel)}/{len(om)} frequencies ({os.cpu_count()} threads) scaled: {t_w:.2f}s; "
+            f"numpy contraction on {len(ks)}/{nkp} k-points, all frequencies, scaled: {t_c:.2f}s; numpy inverse "
+            f"on {len(osel)}/{len(om)} frequencies scaled: {t_i:.2f}s")
     return t_w + t_c + t_i, desc
 
 
@@ -318,13 +370,14 @@ def main():
         gpu_step(inp, s, precision=a.precision)
     barrier()
     timers = []
+    phases = []
     l0 = lib.pg_launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     wall0 = time.time()
     ev0.record(stream)
     for s in range(a.steps):
-        gpu_step(inp, a.warmup + s, timers=timers, precision=a.precision)
+        gpu_step(inp, a.warmup + s, timers=timers, precision=a.precision, phases=phases)
     ev1.record(stream)
     barrier()
     wall1 = time.time()
@@ -364,6 +417,13 @@ def main():
                 "note": "algorithmic flops = 8*N_PB^2*P*Nk*Nw (full complex GEMM count) per launch; "
                         "peak = nominal GB300 FP64 (no measured FP64 figure available)"}
 
+    phase_ms = {name: statistics.mean(e[i].elapsed_time(e[i + 1]) for e in phases)
+                for i, name in enumerate(["weights", "chi0", "eps_inverse"])}
+    fp64 = None
+    if a.precision == "mixed" and a.fp64_k_sample > 0:
+        v64, parts = fp64_gpu_estimate(inp, a.fp64_k_sample)
+        fp64 = {"value": v64, "unit": "s/q-point", **parts}
+
     e2e = None
     if not a.no_e2e:
         out_host = inp.out_h
@@ -402,7 +462,7 @@ def main():
                 "config": {"workload": workload_desc(w), "precision": a.precision, "parallelism": "replicas",
                            "l2": "inputs larger than L2 (matrix elements %.2f GB read every step)"
                                  % (inp.minm_host.numel() * 16 / 1e9)},
-                "roofline": roof, "kernel_status": status_bits,
+                "roofline": roof, "kernel_status": status_bits, "phases_ms": phase_ms, "fp64_gpu": fp64,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks}
         print(json.dumps(line), flush=True)
     if dist is not None:
