@@ -93,11 +93,14 @@ int pg_wings_f64(const void* minm, int nk_chunk, int k0, const double* kcw, int 
  * needed).  omega_batch frequencies share one set of weighted digits
  * (workspace grows with it); kb_split > 0 caps the K-blocks per CTA
  * (0 = automatic).  d_status receives PG_ERR_TIMEOUT if a pipeline wait
- * expired (the result is then invalid). */
+ * expired (the result is then invalid).  gemm_events (may be NULL) holds
+ * 2·ceil(nom/omega_batch) created cudaEvent_t handles; event 2b and 2b+1 are
+ * recorded on `stream` just before and after batch b's digit-GEMM launch, so
+ * a caller can time that kernel alone. */
 size_t pg_chi0_mixed_workspace(int nb1, int nb2, int nkp, int npb, int omega_batch, int kb_split);
 int pg_chi0_mixed(const void* minm, int nkp, const double* kcw, int nb1, int nb2, int nom, int npb, double coef,
                   void* eps, void* work, size_t work_bytes, int omega_batch, int kb_split, unsigned* d_status,
-                  void* stream);
+                  void* stream, void* const* gemm_events);
 /* Workspace layout (byte offsets and sizes) for inspection by tests. */
 int pg_chi0_mixed_layout(int nb1, int nb2, int nkp, int npb, int omega_batch, int kb_split, size_t* offs,
                          long long* dims);

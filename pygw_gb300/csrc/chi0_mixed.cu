@@ -15,20 +15,29 @@
 //     I_d    = Σ_{s+t=d} Σ_K a_s[r,K] b_t[c,K]   (an integer).
 // I_d is accumulated EXACTLY: the tensor core adds integer-valued products
 // into an FP32 TMEM accumulator; every ≤ 14 K-blocks (896 K-values, sum
-// < 2^24) the epilogue warps move the multiples of 2^12 into a second TMEM
+// < 2^24) the epilogue warps move the multiples of 2^12 into an FP32 register
 // accumulator (exact while below 2^36 — the host splits K so it stays
 // below 2^35) and leave the remainder in place.  Each group's integer is
 // then combined in FP64.  The only rounding is the dropped 5th-digit
 // residual and the dropped d ≥ 5 pairs (≈ 1e-11 relative per row scale).
 //
-// Kernel layout: one CTA per 128×128 tile of the upper triangle of G, per
-// frequency, per K-split; warp 0 issues TMA loads (one A-digit and one
-// B-digit 128×64 bf16 tile per stage, 128-byte swizzle, 6 stages), warp 1
-// allocates TMEM and issues tcgen05.mma (M=128, N=128, K=16), warps 2–5
-// renormalise the accumulators.  Two accumulators alternate so the tensor
-// core keeps working while the previous chunk is renormalised.  Every wait
-// is bounded (≈ 5 s of %globaltimer); on expiry the kernel records
-// PG_ERR_TIMEOUT, drains its own in-flight work, frees TMEM and returns.
+// Kernel layout: a cluster of two CTAs owns a 256×256 block of the upper
+// block triangle of G, per frequency, per K-split.  CTA r of the cluster
+// computes the 128-row tile ti = 2·rp + r against the block's 256 columns
+// (one 128×256 tcgen05.mma per 16 K, or 128×128 on the diagonal); the B-digit
+// tile of the block is loaded half by each CTA and multicast to both, so each
+// SM reads 32 KB from L2 per 64-wide K-block for 2·128·256·64 flop.
+// Warp 0 issues the TMA loads (A tile + two B halves per stage, 128-byte
+// swizzle, 4 stages), warp 1 allocates TMEM and issues the MMAs, warps 2–9
+// renormalise: the low accumulators (two 256-column TMEM buffers used in
+// turn, so the tensor core keeps working while the previous chunk is
+// renormalised) and a high accumulator per group held in registers (each
+// epilogue thread owns one row × 128 columns).  A stage is refilled only when
+// the MMAs of both CTAs have read it (each MMA commit arrives on both CTAs'
+// "empty" barriers).  Every wait is bounded (≈ 5 s of %globaltimer); on
+// expiry the kernel records PG_ERR_TIMEOUT, drains its own in-flight work,
+// frees TMEM and returns; the cluster's two CTAs meet at a cluster barrier
+// before either exits, so no multicast lands in a finished CTA.
 #include <cuda_runtime.h>
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -41,20 +50,23 @@
 namespace pgm {
 
 constexpr int S = 5;            // digits per value
-constexpr int TM = 128;         // tile rows (A) = tile cols (B)
+constexpr int TM = 128;         // tile rows (A) = B rows loaded by one CTA
+constexpr int TN = 256;         // columns of a cluster's block
 constexpr int KB = 64;          // K per stage (one 128-byte swizzle row of bf16)
-constexpr int NST = 6;          // pipeline stages
-constexpr int LBLK = 14;        // K-blocks per exact chunk: 14·64·129² + 2^12 < 2^24
-constexpr int TILE_BYTES = TM * KB * 2;           // 16 KB
-constexpr int STAGE_BYTES = 2 * TILE_BYTES;       // A + B
-constexpr int NTHREADS = 192;                     // 6 warps
-constexpr uint32_t TMEM_COLS = 512;
+constexpr int NST = 4;          // pipeline stages
+constexpr int LBLK = 14;        // K-blocks per exact chunk: 14·64·129² + 2^11 < 2^24
+constexpr int CL = 2;           // CTAs per cluster (share the B tile)
+constexpr int TILE_BYTES = TM * KB * 2;           // 16 KB: one 128-row digit tile
+constexpr int STAGE_BYTES = 3 * TILE_BYTES;       // A tile + the two B halves
+constexpr int NEPI = 8;                           // epilogue warps
+constexpr int NTHREADS = 32 * (2 + NEPI);         // 320
+constexpr uint32_t TMEM_COLS = 512;               // two 256-column low accumulators
 constexpr unsigned long long WAIT_NS = 5000000000ull;   // 5 s per wait
 
 struct OzParams {
   double* out;          // [nsplit][wb][npair][128 (col)][128 (row)]
   unsigned* status;
-  int R_pad, nT, npair, nkb, kb_per_split, nsplit, wb;
+  int R_pad, nT, nTv, nC, npair, nkb, kb_per_split, nsplit, wb;
 };
 
 // ------------------------------------------------------------ PTX helpers
@@ -63,6 +75,14 @@ __device__ __forceinline__ unsigned long long gtime() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
@@ -103,10 +123,27 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
       "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
       : "memory");
 }
+// The same tile written at this shared-memory offset in every CTA of `mask`,
+// completing bytes on the barrier at the same offset in each of them.
+__device__ __forceinline__ void tma_load_2d_mc(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y,
+                                               uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1, {%3, "
+      "%4}], [%2], %5;" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y), "h"(mask)
+      : "memory");
+}
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+// Arrive on the barrier at this offset in every CTA of `mask` once this thread's MMAs have completed.
+__device__ __forceinline__ void tc_commit_mc(uint64_t* bar, uint16_t mask) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::
+                   "r"(smem_u32(bar)),
+               "h"(mask)
                : "memory");
 }
 __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
@@ -116,32 +153,37 @@ __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
       : "memory");
 }
-// 32 lanes × 32 consecutive 32-bit columns per warp.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-  uint32_t r[32];
+// 32 lanes × 8 consecutive 32-bit columns per warp.
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
+}
+// 32 lanes × 16 consecutive 32-bit columns per warp.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
-      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
-__device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&v)[32]) {
-  uint32_t r[32];
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
+  uint32_t r[16];
 #pragma unroll
-  for (int i = 0; i < 32; i++) r[i] = __float_as_uint(v[i]);
+  for (int i = 0; i < 16; i++) r[i] = __float_as_uint(v[i]);
   asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
-      "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          taddr),
       "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
-      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]),
-      "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]),
-      "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
       : "memory");
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
@@ -157,13 +199,16 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
   d |= (uint64_t)2 << 61;                             // 128-byte swizzle
   return d;
 }
-// Instruction descriptor, kind::f16: D=F32, A=B=BF16, both K-major, M=128, N=128.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TM >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+// Instruction descriptor, kind::f16: D=F32, A=B=BF16, both K-major, M=128, N=n.
+__host__ __device__ constexpr uint32_t idesc_m128(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+}
 
-__device__ __forceinline__ void tile_pair(int lin, int nT, int& ti, int& tj) {
+// Linear index → (i, j), i ≤ j < n, row-major over the upper triangle.
+__host__ __device__ __forceinline__ void tri_pair(int lin, int n, int& i, int& j) {
   int t = 0, rem = lin;
-  while (rem >= nT - t) { rem -= nT - t; t++; }
-  ti = t; tj = t + rem;
+  while (rem >= n - t) { rem -= n - t; t++; }
+  i = t; j = t + rem;
 }
 
 // ------------------------------------------------------ the digit GEMM
@@ -181,18 +226,26 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   volatile int* abort_flag = (volatile int*)(tmem_base_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int ti, tj;
-  tile_pair(blockIdx.x, p.nT, ti, tj);
+  const int crank = (int)cluster_rank();
+  int rp, cb;
+  tri_pair(blockIdx.x / CL, p.nC, rp, cb);
+  const int ti = 2 * rp + crank;                 // this CTA's 128-row tile
+  // column tiles 2cb, 2cb+1 of the block that lie in the upper triangle and
+  // hold real rows (at least one is computed, so both CTAs issue MMAs)
+  const int n_off = (ti > 2 * cb) ? 1 : 0;
+  int n_tiles = min(2 * cb + 2, p.nTv) - (2 * cb + n_off);
+  if (n_tiles < 1) n_tiles = 1;
   const int wl = blockIdx.y;        // frequency within the batch
   const int split = blockIdx.z;
   const int kb0 = split * p.kb_per_split;
   const int kb1 = min(p.nkb, kb0 + p.kb_per_split);
+  const uint16_t both = (uint16_t)((1u << CL) - 1u);
 
   if (threadIdx.x == 0) {
-    for (int i = 0; i < NST; i++) { mbar_init(full + i, 1); mbar_init(empty + i, 1); }
+    for (int i = 0; i < NST; i++) { mbar_init(full + i, 1); mbar_init(empty + i, CL); }
     // acc_empty / group_done: every epilogue thread arrives (no unbounded named barrier)
-    for (int i = 0; i < 2; i++) { mbar_init(acc_full + i, 1); mbar_init(acc_empty + i, 128); }
-    mbar_init(group_done, 128);
+    for (int i = 0; i < 2; i++) { mbar_init(acc_full + i, 1); mbar_init(acc_empty + i, 32 * NEPI); }
+    mbar_init(group_done, 32 * NEPI);
     mbar_init(drain, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -205,9 +258,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   }
   tc_fence_before();
   __syncthreads();
+  cluster_sync_all();            // the peer's barriers exist before any multicast reaches them
   tc_fence_after();
   const uint32_t tmem = *tmem_base_slot;
-  // column layout: [0,128) low0, [128,256) low1, [256,384) high
   const int nchunk_per_pass = (kb1 - kb0 + LBLK - 1) / LBLK;
 
   if (warp == 0) {
@@ -219,7 +272,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         for (int s = 0; s <= d && ok; s++) {
           const int t = d - s;
           const int ya = s * p.R_pad + ti * TM;
-          const int yb = (wl * S + t) * p.R_pad + tj * TM;
+          const int yb = (wl * S + t) * p.R_pad + cb * TN + crank * TM;
           for (int kb = kb0; kb < kb1 && ok; kb++, it++) {
             const int st = it % NST;
             if (it >= NST) ok = mbar_wait(empty + st, ((it / NST) - 1) & 1, abort_flag, p.status);
@@ -227,20 +280,22 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             unsigned char* sa = smem + st * STAGE_BYTES;
             mbar_expect_tx(full + st, STAGE_BYTES);
             tma_load_2d(sa, &tmA, full + st, kb * KB, ya);
-            tma_load_2d(sa + TILE_BYTES, &tmB, full + st, kb * KB, yb);
+            tma_load_2d_mc(sa + TILE_BYTES * (1 + crank), &tmB, full + st, kb * KB, yb, both);
           }
         }
-      // drain: every stage issued must have landed before the CTA exits
+      // drain: the last phase of every stage must have been read by both CTAs'
+      // MMAs (so every load and every remote arrival on this CTA has landed)
       const int issued = it;
+      const unsigned long long t0 = gtime();
       for (int j = max(0, issued - NST); j < issued; j++) {
         const int st = j % NST;
-        const unsigned long long t0 = gtime();
-        while (!mbar_test(full + st, (j / NST) & 1) && gtime() - t0 < WAIT_NS) {}
+        while (!mbar_test(empty + st, (j / NST) & 1) && gtime() - t0 < WAIT_NS) {}
       }
     }
   } else if (warp == 1) {
     // ---------------------------------------------------------- MMA issuer
     if (lane == 0 && kb1 > kb0) {
+      const uint32_t idesc = idesc_m128(TM * n_tiles);
       int it = 0, c = 0;
       bool ok = true;
       for (int d = 0; d < S && ok; d++) {
@@ -253,7 +308,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             if (c >= 2) ok = mbar_wait(acc_empty + b, ((c >> 1) - 1) & 1, abort_flag, p.status);
             if (!ok) break;
             tc_fence_after();
-            const uint32_t dcol = tmem + (uint32_t)(b * TM);
+            const uint32_t dcol = tmem + (uint32_t)(b * TN + n_off * TM);
             const int cb0 = kb0 + ch * LBLK, cb1 = min(kb1, cb0 + LBLK);
             for (int kb = cb0; kb < cb1; kb++, it++) {
               const int st = it % NST;
@@ -261,13 +316,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               if (!ok) break;
               tc_fence_after();
               const uint32_t sa = smem_u32(smem + st * STAGE_BYTES);
-              const uint64_t ad = sdesc_sw128(sa), bd = sdesc_sw128(sa + TILE_BYTES);
+              const uint64_t ad = sdesc_sw128(sa), bd = sdesc_sw128(sa + TILE_BYTES * (1 + n_off));
 #pragma unroll
               for (int k = 0; k < KB / 16; k++) {
                 const uint32_t accumulate = (used[b] || kb > cb0 || k > 0) ? 1u : 0u;
-                tc_mma(dcol, ad + (uint64_t)(2 * k), bd + (uint64_t)(2 * k), IDESC, accumulate);
+                tc_mma(dcol, ad + (uint64_t)(2 * k), bd + (uint64_t)(2 * k), idesc, accumulate);
               }
-              tc_commit(empty + st);     // stage free once these MMAs have read it
+              tc_commit_mc(empty + st, both);   // stage free in both CTAs once these MMAs have read it
             }
             if (!ok) break;
             used[b] = true;
@@ -281,53 +336,62 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       while (!mbar_test(drain, 0) && gtime() - t0 < WAIT_NS) {}
     }
   } else {
-    // ---------------------------------------------------------- epilogue (warps 2–5)
+    // ---------------------------------------------------------- epilogue (warps 2–9)
     const int q = warp & 3;                        // TMEM lane quarter this warp may access
+    const int h = (warp - 2) >> 2;                 // column half of the block
     const int row = q * 32 + lane;                 // accumulator row (A tile row)
-    const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-    const uint32_t t_low0 = tmem + lane_off, t_low1 = tmem + lane_off + TM, t_high = tmem + lane_off + 2 * TM;
-    double* out = p.out + ((((size_t)split * p.wb + wl) * p.npair + blockIdx.x) * TM) * TM;
+    const int tj = 2 * cb + h;
+    const bool active = h >= n_off && h < n_off + n_tiles;
+    const bool stored = tj >= ti;                  // tile (ti, tj) is kept (upper triangle)
+    const uint32_t t_b0 = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * TM);
+    const uint32_t t_b1 = t_b0 + TN;
+    const int pair = stored ? ti * p.nT - ti * (ti - 1) / 2 + (tj - ti) : 0;
+    double* out = p.out + ((((size_t)split * p.wb + wl) * p.npair + pair) * TM) * TM;
+    float hi[TM];                                  // high accumulator: multiples of 2^12, exact below 2^36
     int c = 0;
     bool ok = kb1 > kb0;
     for (int d = 0; d < S && ok; d++) {
-      bool used[2] = {false, false};
-      bool high_init = false;
+#pragma unroll
+      for (int i = 0; i < TM; i++) hi[i] = 0.0f;
       const int nchunks_group = (d + 1) * nchunk_per_pass;
+      const int c_first = c;
       for (int gc = 0; gc < nchunks_group && ok; gc++, c++) {
         const int b = c & 1;
         ok = mbar_wait(acc_full + b, (c >> 1) & 1, abort_flag, p.status);
         if (!ok) break;
         tc_fence_after();
-        const uint32_t tl = b ? t_low1 : t_low0;
-        for (int cb = 0; cb < TM; cb += 32) {
-          float lo[32], hi[32];
-          tmem_ld32(tl + cb, lo);
-          if (high_init) tmem_ld32(t_high + cb, hi);
+        if (active) {
+          const uint32_t tl = b ? t_b1 : t_b0;
 #pragma unroll
-          for (int i = 0; i < 32; i++) {
-            const float h = rintf(lo[i] * (1.0f / 4096.0f)) * 4096.0f;   // multiple of 2^12
-            lo[i] = lo[i] - h;                                            // |residual| ≤ 2^11
-            hi[i] = high_init ? hi[i] + h : h;                            // exact below 2^36
+          for (int cc = 0; cc < TM / 16; cc++) {
+            float lo[16];
+            tmem_ld16(tl + cc * 16, lo);
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+              const float hh = rintf(lo[i] * (1.0f / 4096.0f)) * 4096.0f;   // multiple of 2^12
+              lo[i] = lo[i] - hh;                                            // |residual| ≤ 2^11
+              hi[cc * 16 + i] += hh;
+            }
+            tmem_st16(tl + cc * 16, lo);
           }
-          tmem_st32(tl + cb, lo);
-          tmem_st32(t_high + cb, hi);
         }
-        high_init = true;
-        used[b] = true;
-        if (gc == nchunks_group - 1) {
-          // group complete: I_d = high + low0 + low1 (exact in FP64), scaled by 2^(−8d)
+        if (gc == nchunks_group - 1 && active) {
+          // group complete: I_d = high + both low remainders (|r| ≤ 2^11, so r0 + r1 is
+          // exact in FP32 and high + r0 + r1 exact in FP64), scaled by 2^(−8d);
+          // 8 columns at a time keep the live registers to hi[] + 16
+          const bool used0 = nchunks_group >= 2 || (c_first & 1) == 0;
+          const bool used1 = nchunks_group >= 2 || (c_first & 1) == 1;
           const double scale = ldexp(1.0, -8 * d);
-          for (int cb = 0; cb < TM; cb += 32) {
-            float h[32], l0[32], l1[32];
-            tmem_ld32(t_high + cb, h);
-            if (used[0]) tmem_ld32(t_low0 + cb, l0);
-            if (used[1]) tmem_ld32(t_low1 + cb, l1);
 #pragma unroll
-            for (int i = 0; i < 32; i++) {
-              double v = (double)h[i];
-              if (used[0]) v += (double)l0[i];
-              if (used[1]) v += (double)l1[i];
-              double& o = out[(size_t)(cb + i) * TM + row];
+          for (int cc = 0; cc < TM / 8; cc++) {
+            float l0[8], l1[8];
+            if (used0) tmem_ld8(t_b0 + cc * 8, l0);
+            if (used1) tmem_ld8(t_b1 + cc * 8, l1);
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+              const float r = (used0 ? l0[i] : 0.0f) + (used1 ? l1[i] : 0.0f);
+              const double v = (double)hi[cc * 8 + i] + (double)r;
+              double& o = out[(size_t)(cc * 8 + i) * TM + row];
               o = (d == 0) ? v * scale : o + v * scale;
             }
           }
@@ -337,14 +401,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (gc == nchunks_group - 1) mbar_arrive(group_done);
       }
     }
-    if (kb1 <= kb0) {
-      for (int i = 0; i < TM; i++) out[(size_t)i * TM + row] = 0.0;        // empty K-split
-    } else if (!ok) {
+    if (stored && (!active || kb1 <= kb0)) {
+      for (int i = 0; i < TM; i++) out[(size_t)i * TM + row] = 0.0;        // padding tile or empty K-split
+    } else if (stored && !ok) {
       for (int i = 0; i < TM; i++) out[(size_t)i * TM + row] = __longlong_as_double(0x7ff8dead00000000LL);
     }
   }
   tc_fence_before();
   __syncthreads();
+  cluster_sync_all();            // neither CTA leaves while the other may still write to it
   tc_fence_after();
   if (warp == 1) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
@@ -445,28 +510,57 @@ __global__ void k_weights_prep(const double* __restrict__ kcw, int nb1, int nb2,
   }
 }
 
-// Exact row maxima of |V_trunc·c·w| per frequency (V relative to 2^eA), as
-// float bits: nonnegative floats order like unsigned integers.
+// Four consecutive bf16 digits (8 bytes) as floats.
+__device__ __forceinline__ void ld_bf16x4(const __nv_bfloat16* p, float (&v)[4]) {
+  const uint2 u = *reinterpret_cast<const uint2*>(p);
+  v[0] = __uint_as_float(u.x << 16);
+  v[1] = __uint_as_float(u.x & 0xffff0000u);
+  v[2] = __uint_as_float(u.y << 16);
+  v[3] = __uint_as_float(u.y & 0xffff0000u);
+}
+// Four floats holding integers |d| ≤ 256 (exact in bf16) stored as 8 bytes.
+__device__ __forceinline__ void st_bf16x4(__nv_bfloat16* p, const float (&v)[4]) {
+  uint2 u;
+  u.x = (__float_as_uint(v[0]) >> 16) | (__float_as_uint(v[1]) & 0xffff0000u);
+  u.y = (__float_as_uint(v[2]) >> 16) | (__float_as_uint(v[3]) & 0xffff0000u);
+  *reinterpret_cast<uint2*>(p) = u;
+}
+
+// Exact row maxima of |V_trunc·c·w| for every frequency of the batch (V relative
+// to 2^eA), as float bits: nonnegative floats order like unsigned integers.
+// One pass over the A digits serves all nw frequencies; 4 K-values per thread.
 __global__ void k_rowmax_B(const __nv_bfloat16* __restrict__ adig, const float2* __restrict__ wpair, int R, int R_pad,
-                           long long K_pad, unsigned* rmax) {
-  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int r = blockIdx.y, wl = blockIdx.z;
-  float m = 0.0f;
-  if (k < K_pad && r < R) {
-    const float a0 = __bfloat162float(adig[((size_t)0 * R_pad + r) * K_pad + k]);
-    const float a1 = __bfloat162float(adig[((size_t)1 * R_pad + r) * K_pad + k]);
-    const float a2 = __bfloat162float(adig[((size_t)2 * R_pad + r) * K_pad + k]);
-    const float vhi = (a0 * 0x1p-8f + a1 * 0x1p-16f) + a2 * 0x1p-24f;
-    m = __fmul_ru(fabsf(vhi), fabsf(wpair[(size_t)wl * K_pad + k].x));
+                           long long K_pad, int nw, unsigned* rmax) {
+  const long long k0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+  const int r = blockIdx.y;
+  const bool in = k0 < K_pad && r < R;
+  float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  if (in) {
+    float a0[4], a1[4], a2[4];
+    ld_bf16x4(adig + ((size_t)0 * R_pad + r) * K_pad + k0, a0);
+    ld_bf16x4(adig + ((size_t)1 * R_pad + r) * K_pad + k0, a1);
+    ld_bf16x4(adig + ((size_t)2 * R_pad + r) * K_pad + k0, a2);
+#pragma unroll
+    for (int j = 0; j < 4; j++) v[j] = fabsf((a0[j] * 0x1p-8f + a1[j] * 0x1p-16f) + a2[j] * 0x1p-24f);
   }
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  __shared__ float sm[8];
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float mm = sm[0];
-    for (int i = 1; i < (int)(blockDim.x >> 5); i++) mm = fmaxf(mm, sm[i]);
-    if (mm > 0.0f) atomicMax(rmax + (size_t)wl * R_pad + r, __float_as_uint(mm));
+  __shared__ float sm[32];
+  for (int wl = 0; wl < nw; wl++) {
+    float m = 0.0f;
+    if (in) {
+      const float4* wp = reinterpret_cast<const float4*>(wpair + (size_t)wl * K_pad + k0);
+      const float4 w01 = wp[0], w23 = wp[1];
+      m = fmaxf(fmaxf(__fmul_ru(v[0], fabsf(w01.x)), __fmul_ru(v[1], fabsf(w01.z))),
+                fmaxf(__fmul_ru(v[2], fabsf(w23.x)), __fmul_ru(v[3], fabsf(w23.z))));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float mm = sm[0];
+      for (int i = 1; i < (int)(blockDim.x >> 5); i++) mm = fmaxf(mm, sm[i]);
+      if (mm > 0.0f) atomicMax(rmax + (size_t)wl * R_pad + r, __float_as_uint(mm));
+    }
+    __syncthreads();
   }
 }
 
@@ -489,29 +583,45 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bb)) + (b - bb);
 }
 __global__ void k_digits_B(const __nv_bfloat16* __restrict__ adig, const int* eA, const float2* __restrict__ wpair,
-                           const int* fB, int R, int R_pad, long long K_pad, int wb, __nv_bfloat16* bdig) {
-  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int r = blockIdx.y, wl = blockIdx.z;
-  if (k >= K_pad) return;
-  float a[S];
+                           const int* fB, int R, int R_pad, long long K_pad, int nw, __nv_bfloat16* bdig) {
+  const long long k0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+  const int r = blockIdx.y;
+  if (k0 >= K_pad) return;
+  float vhi[4], vlo[4];
+  {
+    float a[S][4];
 #pragma unroll
-  for (int s = 0; s < S; s++) a[s] = __bfloat162float(adig[((size_t)s * R_pad + r) * K_pad + k]);
-  const float vhi = ((a[0] * 0x1p-8f + a[1] * 0x1p-16f) + a[2] * 0x1p-24f);   // exact
-  const float vlo = (a[3] * 0x1p-32f + a[4] * 0x1p-40f);                       // exact
-  const float2 w = wpair[(size_t)wl * K_pad + k];
-  const float ph = vhi * w.x;
-  const float pe = fmaf(vhi, w.x, -ph);
-  const float pl = pe + (vhi * w.y + vlo * w.x);
-  const int sh = (r < R) ? (eA[r] - fB[(size_t)wl * R_pad + r]) : 0;
-  float yh = ldexpf(ph, sh), yl = ldexpf(pl, sh);
-  two_sum(yh, yl, yh, yl);
+    for (int s = 0; s < S; s++) ld_bf16x4(adig + ((size_t)s * R_pad + r) * K_pad + k0, a[s]);
 #pragma unroll
-  for (int s = 0; s < S; s++) {
-    const float t = yh * 256.0f;
-    const float dg = rintf(t);
-    const float rh = t - dg;              // exact
-    two_sum(rh, yl * 256.0f, yh, yl);
-    bdig[(((size_t)wl * S + s) * R_pad + r) * K_pad + k] = __float2bfloat16_rn(dg);
+    for (int j = 0; j < 4; j++) {
+      vhi[j] = ((a[0][j] * 0x1p-8f + a[1][j] * 0x1p-16f) + a[2][j] * 0x1p-24f);   // exact
+      vlo[j] = (a[3][j] * 0x1p-32f + a[4][j] * 0x1p-40f);                         // exact
+    }
+  }
+  for (int wl = 0; wl < nw; wl++) {
+    const float4* wp = reinterpret_cast<const float4*>(wpair + (size_t)wl * K_pad + k0);
+    const float4 w01 = wp[0], w23 = wp[1];
+    const float wh[4] = {w01.x, w01.z, w23.x, w23.z}, wo[4] = {w01.y, w01.w, w23.y, w23.w};
+    const int sh = (r < R) ? (eA[r] - fB[(size_t)wl * R_pad + r]) : 0;
+    float dg[S][4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const float ph = vhi[j] * wh[j];
+      const float pe = fmaf(vhi[j], wh[j], -ph);
+      const float pl = pe + (vhi[j] * wo[j] + vlo[j] * wh[j]);
+      float yh = ldexpf(ph, sh), yl = ldexpf(pl, sh);
+      two_sum(yh, yl, yh, yl);
+#pragma unroll
+      for (int s = 0; s < S; s++) {
+        const float t = yh * 256.0f;
+        const float d = rintf(t);
+        const float rh = t - d;              // exact
+        two_sum(rh, yl * 256.0f, yh, yl);
+        dg[s][j] = d;
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < S; s++) st_bf16x4(bdig + (((size_t)wl * S + s) * R_pad + r) * K_pad + k0, dg[s]);
   }
 }
 
@@ -546,7 +656,7 @@ static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct MixedLayout {
   long long K, K_pad;
-  int N, R, R_pad, nT, npair, nkb, nsplit, kb_per_split, wb;
+  int N, R, R_pad, nT, nTv, nC, nitems, npair, nkb, nsplit, kb_per_split, wb;
   size_t off_adig, off_bdig, off_tmax, off_wpair, off_rmax, off_eA, off_fB, off_out, total;
 };
 
@@ -557,9 +667,12 @@ static MixedLayout mixed_layout(int nb1, int nb2, int nkp, int npb, int wb, int 
   L.nkb = (int)(L.K_pad / KB);
   L.N = npb;
   L.R = 2 * npb;
-  L.R_pad = (L.R + TM - 1) / TM * TM;
-  L.nT = L.R_pad / TM;
-  L.npair = L.nT * (L.nT + 1) / 2;
+  L.R_pad = (L.R + TN - 1) / TN * TN;       // whole 256-column blocks
+  L.nT = L.R_pad / TM;                      // 128-row tiles (even)
+  L.nTv = (L.R + TM - 1) / TM;              // tiles holding real rows
+  L.nC = L.R_pad / TN;                      // 256-column blocks
+  L.nitems = L.nC * (L.nC + 1) / 2;         // upper-triangle blocks, one cluster each
+  L.npair = L.nT * (L.nT + 1) / 2;          // stored 128×128 tiles
   // Exact-range split: a group sum over one split stays below 2^35
   // (5 pairs · kb·64 · 129² < 2^35  →  kb ≤ 6452).
   const int kb_max = (kb_split > 0 && kb_split < 6400) ? kb_split : 6400;
@@ -614,9 +727,10 @@ extern "C" size_t pg_chi0_mixed_workspace(int nb1, int nb2, int nkp, int npb, in
 // Writes the full Hermitian χ0 (before symmetrisation, +1 and inversion) to
 // eps[ω][J][I].  Frequencies are processed omega_batch at a time; kb_split
 // (> 0) caps the 64-value K-blocks one CTA sums (0 = the largest exact range).
+// gemm_events (optional): 2 per batch, recorded around each digit-GEMM launch.
 extern "C" int pg_chi0_mixed(const void* minm, int nkp, const double* kcw, int nb1, int nb2, int nom, int npb,
                              double coef, void* eps, void* work, size_t work_bytes, int omega_batch, int kb_split,
-                             unsigned* d_status, void* stream) {
+                             unsigned* d_status, void* stream, void* const* gemm_events) {
   if (!minm || !kcw || !eps || !work || nkp <= 0 || nb1 <= 0 || nb2 <= 0 || nom <= 0 || npb <= 0 || omega_batch <= 0)
     return PG_EARG;
   const int wb = omega_batch < nom ? omega_batch : nom;
@@ -651,19 +765,33 @@ extern "C" int pg_chi0_mixed(const void* minm, int nkp, const double* kcw, int n
   if (cudaFuncSetAttribute(k_ozaki_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return PG_ECUDA;
   OzParams op;
-  op.out = out; op.status = d_status; op.R_pad = L.R_pad; op.nT = L.nT; op.npair = L.npair; op.nkb = L.nkb;
-  op.kb_per_split = L.kb_per_split; op.nsplit = L.nsplit;
+  op.out = out; op.status = d_status; op.R_pad = L.R_pad; op.nT = L.nT; op.nTv = L.nTv; op.nC = L.nC;
+  op.npair = L.npair; op.nkb = L.nkb; op.kb_per_split = L.kb_per_split; op.nsplit = L.nsplit; op.wb = wb;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
   for (int om0 = 0; om0 < nom; om0 += wb) {
     const int nw = (om0 + wb <= nom) ? wb : nom - om0;
-    op.wb = wb;
     k_weights_prep<<<dim3(L.nkb, nw), 64, 0, s>>>(kcw, nb1, nb2, nkp, om0, nw, coef, L.K, L.K_pad, wpair);
     if (cudaMemsetAsync(rmax, 0, (size_t)L.wb * L.R_pad * 4, s) != cudaSuccess) return PG_ECUDA;
-    k_rowmax_B<<<dim3((unsigned)((L.K_pad + 255) / 256), L.R_pad, nw), 256, 0, s>>>(adig, wpair, L.R, L.R_pad,
-                                                                                   L.K_pad, rmax);
+    k_rowmax_B<<<dim3((unsigned)((L.K_pad + 1023) / 1024), L.R_pad), 256, 0, s>>>(adig, wpair, L.R, L.R_pad, L.K_pad,
+                                                                                  nw, rmax);
     k_row_exp_B<<<(nw * L.R_pad + 255) / 256, 256, 0, s>>>(rmax, eA, L.R, L.R_pad, nw, fB);
-    k_digits_B<<<dim3((unsigned)((L.K_pad + 255) / 256), L.R_pad, nw), 256, 0, s>>>(adig, eA, wpair, fB, L.R, L.R_pad,
-                                                                                   L.K_pad, nw, bdig);
-    k_ozaki_gemm<<<dim3(L.npair, nw, L.nsplit), NTHREADS, smem, s>>>(mapA, mapB, op);
+    k_digits_B<<<dim3((unsigned)((L.K_pad + 1023) / 1024), L.R_pad), 256, 0, s>>>(adig, eA, wpair, fB, L.R, L.R_pad,
+                                                                                  L.K_pad, nw, bdig);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(CL * L.nitems), (unsigned)nw, (unsigned)L.nsplit);
+    cfg.blockDim = dim3(NTHREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const int batch = om0 / wb;
+    if (gemm_events && cudaEventRecord((cudaEvent_t)gemm_events[2 * batch], s) != cudaSuccess) return PG_ECUDA;
+    if (cudaLaunchKernelEx(&cfg, k_ozaki_gemm, mapA, mapB, op) != cudaSuccess) return PG_ECUDA;
+    if (gemm_events && cudaEventRecord((cudaEvent_t)gemm_events[2 * batch + 1], s) != cudaSuccess) return PG_ECUDA;
     k_assemble<<<dim3((npb + 127) / 128, npb, nw), 128, 0, s>>>(out, eA, fB, npb, L.R_pad, L.nT, L.npair, L.nsplit,
                                                                wb, om0, (double2*)eps);
     pg_count_launches(6);

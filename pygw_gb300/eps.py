@@ -13,6 +13,8 @@ synthetic generator here) gets the same data flow.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import torch
 
@@ -176,9 +178,11 @@ def mixed_omega_batch(nb1, nb2, nkp, npb, nom, budget_bytes=None):
 
 
 def chi0_mixed(kcw_d, minm, nkp, npb, nb1, nb2, nom, omega_batch=None, kb_split=0, stream=None, work=None,
-               timers=None):
+               timers=None, gemm_timers=None):
     """Split-precision χ0 (tensor cores) for all frequencies: returns
-    ``(eps, status, work)`` with the full Hermitian χ0 in ``eps`` [nom][N][N]."""
+    ``(eps, status, work)`` with the full Hermitian χ0 in ``eps`` [nom][N][N].
+    ``timers`` receives one (start, end) event pair around the whole call,
+    ``gemm_timers`` one pair per frequency batch around the digit-GEMM kernel."""
     lib = _lib.load()
     P = nb1 * nb2
     m = _all_k_device(minm, nkp, P, npb)
@@ -193,12 +197,22 @@ def chi0_mixed(kcw_d, minm, nkp, npb, nb1, nb2, nom, omega_batch=None, kb_split=
     if timers is not None:
         ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
         ev[0].record(s)
+    gev = None
+    if gemm_timers is not None:
+        nbatch = -(-nom // min(wb, nom))
+        gev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * nbatch)]
+        for e in gev:
+            e.record(s)                          # creates the CUDA event behind each object
+        handles = (ctypes.c_void_p * len(gev))(*[e.cuda_event for e in gev])
     rc = lib.pg_chi0_mixed(ptr(m), nkp, ptr(kcw_d), nb1, nb2, nom, npb, -FSPIN, ptr(eps), ptr(work), work.numel(),
-                           int(wb), int(kb_split), ptr(status), stream_handle(stream))
+                           int(wb), int(kb_split), ptr(status), stream_handle(stream),
+                           handles if gev is not None else None)
     _lib.check(rc, "pg_chi0_mixed")
     if ev is not None:
         ev[1].record(s)
         timers.append(ev)
+    if gev is not None:
+        gemm_timers.extend((gev[2 * b], gev[2 * b + 1]) for b in range(len(gev) // 2))
     return eps, status, work
 
 
