@@ -50,6 +50,7 @@ struct Params {
   const double* omega; // [nom]
   const int* tetc;     // [ntet][4]: tetc[i + 4*t]
   double* scratch;     // [ntet][4][nomc][P]
+  const int* order;    // items sorted by polyhedron class (null: natural order)
   unsigned* status;    // device status word (may be null)
   unsigned long long* counters;  // PG_NCOUNTERS (may be null)
   double ef;
@@ -906,37 +907,35 @@ __device__ void subtet_one_omega(SubTet& s, const double e[4], const double f[4]
   for (int c = 0; c < 4; c++) acc[c] = first ? (0.0 + wo[c]) : (acc[c] + wo[c]);
 }
 
-__global__ void __launch_bounds__(128) k_tet_weights(Params p) {
-  const int P = p.nb1 * p.nb2;
-  const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (item >= (long long)P * p.ntet) return;
-  const int tet = (int)(item / P);
-  const int pair = (int)(item - (long long)tet * P);
-  const int ib = pair % p.nb1;
-  const int jb = pair / p.nb1;
-  const int lt = 6 * p.kqid[tet / 6] + tet % 6;   // linked k−q tetrahedron (for_tetrahedra.f90:426-432)
+// Corner energies of item (tetrahedron, band pair) and its integration
+// polyhedron: surfnodes → unrepnodes → relnodes → sortnodes
+// (for_tetrahedra3.f90:3-136 up to the nnod dispatch).  Returns true when
+// the item contributes zero (skipped by the reference's tests at
+// for_tetrahedra.f90:447/452, fewer than 4 nodes, or a geometry error).
+struct Item {
+  int tet, pair;
   double e[4], f[4];
+};
+__device__ bool item_geometry(const Params& p, long long item, Item& it, Nodes& N, int index[9][2], Ctx& cx) {
+  const int P = p.nb1 * p.nb2;
+  it.tet = (int)(item / P);
+  it.pair = (int)(item - (long long)it.tet * P);
+  const int ib = it.pair % p.nb1;
+  const int jb = it.pair / p.nb1;
+  const int lt = 6 * p.kqid[it.tet / 6] + it.tet % 6;   // linked k−q tetrahedron (for_tetrahedra.f90:426-432)
 #pragma unroll
   for (int i = 0; i < 4; i++) {
-    e[i] = p.enk[(size_t)ib + (size_t)p.nbnd * p.tetc[i + 4 * tet]];
-    f[i] = p.enk[(size_t)(jb + p.ncg + p.numin) + (size_t)p.nbnd * p.tetc[i + 4 * lt]];
+    it.e[i] = p.enk[(size_t)ib + (size_t)p.nbnd * p.tetc[i + 4 * it.tet]];
+    it.f[i] = p.enk[(size_t)(jb + p.ncg + p.numin) + (size_t)p.nbnd * p.tetc[i + 4 * lt]];
   }
-  const size_t wstride = (size_t)P;
-  const size_t cstride = (size_t)p.nomc * P;
-  double* out = p.scratch + (size_t)tet * 4 * cstride + pair;
-  Ctx cx;
-  cx.status = 0;
-  for (int i = 0; i < PG_NCOUNTERS; i++) cx.cnt[i] = 0;
-  const double fhi = fmax(fmax(f[0], f[1]), fmax(f[2], f[3]));
-  const double emin = fmin(fmin(e[0], e[1]), fmin(e[2], e[3]));
+  const double fhi = fmax(fmax(it.f[0], it.f[1]), fmax(it.f[2], it.f[3]));
+  const double emin = fmin(fmin(it.e[0], it.e[1]), fmin(it.e[2], it.e[3]));
   bool zero = (fhi <= p.ef) || (emin > p.ef);   // for_tetrahedra.f90:447, 452
-  int index[9][2];
-  Nodes N;
   if (!zero) {
     cx.cnt[PG_CNT_CALLS]++;
-    surfnodes(N, e, f, p.ef);
+    surfnodes(N, it.e, it.f, p.ef);
     unrepnodes(N);
-    if (relnodes(N, e, f, p.ef) != 0) { cx.status |= PG_ERR_RELNODES; zero = true; }
+    if (relnodes(N, it.e, it.f, p.ef) != 0) { cx.status |= PG_ERR_RELNODES; zero = true; }
     else if (N.nnod > 8) { cx.status |= PG_ERR_NNOD; zero = true; }
     else if (sortnodes(N, index, cx) != 0) { zero = true; }
     else {
@@ -944,6 +943,114 @@ __global__ void __launch_bounds__(128) k_tet_weights(Params p) {
       if (N.nnod < 4) zero = true;
     }
   }
+  return zero;
+}
+
+// Corners of the pentahedron (5) / prism (6) — two of them for 7 and 8 nodes —
+// from the node order sortnodes produced (genericfunf_par / genericprism_par
+// inputs, for_tetrahedra3.f90:60-131).
+__device__ void place_nodes(const Nodes& N, const int index[9][2], double tc[2][6][3], Ctx& cx) {
+  const int nnod = N.nnod;
+  const int cap = (nnod == 5 || nnod == 7) ? 5 : 6;
+  const int ngroup = (nnod >= 7) ? 2 : 1;
+  bool written[6] = {false, false, false, false, false, false};
+  for (int a = 0; a < 6; a++) for (int c = 0; c < 3; c++) tc[0][a][c] = tc[1][a][c] = 0.0;
+  for (int g = 0; g < ngroup; g++) {
+    if (g == 1) for (int a = 0; a < 6; a++) for (int c = 0; c < 3; c++) tc[1][a][c] = tc[0][a][c];
+    for (int inod = 1; inod <= nnod; inod++) {
+      const int pos = index[inod][g];
+      if (ngroup == 2 && pos == 0) continue;
+      if (pos < 1 || pos > cap) { cx.status |= PG_ERR_UNDEFINED; continue; }
+      for (int c = 0; c < 3; c++) tc[g][pos - 1][c] = N.x[inod][c];
+      written[pos - 1] = true;
+    }
+    for (int a = 0; a < cap; a++) if (!written[a]) cx.status |= PG_ERR_UNDEFINED;
+  }
+}
+
+// Class of an item for the work sort: 0 = contributes zero; otherwise
+// 1 + 6·(nnod − 4) + grouping of its first sub-tetrahedron (0: below the
+// volume tolerance, 1..5: sorteq case 4/6/8/10/16).  Items of one class run
+// the same code path, so sorting by class keeps warps converged.
+constexpr int NCLASS = 32;
+__device__ int item_class(const Params& p, long long item) {
+  Ctx cx;
+  cx.status = 0;
+  for (int i = 0; i < PG_NCOUNTERS; i++) cx.cnt[i] = 0;
+  Item it;
+  Nodes N;
+  int index[9][2];
+  if (item_geometry(p, item, it, N, index, cx) || cx.status) return 0;
+  SubTet s;
+  if (N.nnod == 4) {
+    for (int n = 0; n < 4; n++) for (int c = 0; c < 3; c++) s.corner[n][c] = N.x[n + 1][c];
+  } else {
+    double tc[2][6][3];
+    place_nodes(N, index, tc, cx);
+    for (int n = 0; n < 4; n++) for (int c = 0; c < 3; c++) s.corner[n][c] = tc[0][n][c];
+  }
+  setup_subtet(s, it.e, it.f, cx);
+  const int g = (s.vol < ZTOL_VOL) ? 0 : s.flag == 4 ? 1 : s.flag == 6 ? 2 : s.flag == 8 ? 3 : s.flag == 10 ? 4 : 5;
+  return 1 + 6 * (N.nnod - 4) + g;
+}
+
+__global__ void __launch_bounds__(128) k_tet_classify(Params p, long long nitems, unsigned char* cls,
+                                                      unsigned* hist) {
+  __shared__ unsigned h[NCLASS];
+  if (threadIdx.x < NCLASS) h[threadIdx.x] = 0;
+  __syncthreads();
+  const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item < nitems) {
+    const int c = item_class(p, item);
+    cls[item] = (unsigned char)c;
+    atomicAdd(&h[c], 1u);
+  }
+  __syncthreads();
+  if (threadIdx.x < NCLASS && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+}
+
+// Exclusive prefix of the class histogram → per-class write cursors.
+__global__ void k_class_offsets(const unsigned* hist, unsigned* cursor) {
+  if (threadIdx.x == 0) {
+    unsigned acc = 0;
+    for (int c = 0; c < NCLASS; c++) { cursor[c] = acc; acc += hist[c]; }
+  }
+}
+
+// order[cursor[class]++] = item, one atomic per (warp, class).  The order
+// within a class is arbitrary; results do not depend on it (every item
+// writes only its own slots, counters are integer sums).
+__global__ void k_class_scatter(const unsigned char* cls, long long nitems, unsigned* cursor, int* order) {
+  const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool in = item < nitems;
+  const int c = in ? cls[item] : -1;
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned peers = __match_any_sync(0xffffffffu, c);
+  const unsigned leader = __ffs(peers) - 1;
+  const unsigned rank = __popc(peers & ((1u << lane) - 1u));
+  unsigned base = 0;
+  if (in && lane == leader) base = atomicAdd(&cursor[c], (unsigned)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  if (in) order[base + rank] = (int)item;
+}
+
+__global__ void __launch_bounds__(128) k_tet_weights(Params p) {
+  const int P = p.nb1 * p.nb2;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)P * p.ntet) return;
+  const long long item = p.order ? (long long)p.order[idx] : idx;
+  Ctx cx;
+  cx.status = 0;
+  for (int i = 0; i < PG_NCOUNTERS; i++) cx.cnt[i] = 0;
+  Item it;
+  Nodes N;
+  int index[9][2];
+  bool zero = item_geometry(p, item, it, N, index, cx);
+  const double* e = it.e;
+  const double* f = it.f;
+  const size_t wstride = (size_t)P;
+  const size_t cstride = (size_t)p.nomc * P;
+  double* out = p.scratch + (size_t)it.tet * 4 * cstride + it.pair;
   if (zero) {
     for (int w = 0; w < p.nomc; w++)
       for (int c = 0; c < 4; c++) out[c * cstride + w * wstride] = 0.0;
@@ -955,24 +1062,11 @@ __global__ void __launch_bounds__(128) k_tet_weights(Params p) {
         for (int c = 0; c < 3; c++) s.corner[n][c] = N.x[n + 1][c];
       subtet_all_omega(s, e, f, p, out, cstride, wstride, 0, cx);
     } else {
-      // Place the nodes into the pentahedron (5) / prism (6) corner lists.
       const int cap = (nnod == 5 || nnod == 7) ? 5 : 6;
       const int nsub = cap - 3;                     // 2 tets per pentahedron, 3 per prism
       const int ngroup = (nnod >= 7) ? 2 : 1;
       double tc[2][6][3];
-      bool written[6] = {false, false, false, false, false, false};
-      for (int a = 0; a < 6; a++) for (int c = 0; c < 3; c++) tc[0][a][c] = tc[1][a][c] = 0.0;
-      for (int g = 0; g < ngroup; g++) {
-        if (g == 1) for (int a = 0; a < 6; a++) for (int c = 0; c < 3; c++) tc[1][a][c] = tc[0][a][c];
-        for (int inod = 1; inod <= nnod; inod++) {
-          const int pos = index[inod][g];
-          if (ngroup == 2 && pos == 0) continue;
-          if (pos < 1 || pos > cap) { cx.status |= PG_ERR_UNDEFINED; continue; }
-          for (int c = 0; c < 3; c++) tc[g][pos - 1][c] = N.x[inod][c];
-          written[pos - 1] = true;
-        }
-        for (int a = 0; a < cap; a++) if (!written[a]) cx.status |= PG_ERR_UNDEFINED;
-      }
+      place_nodes(N, index, tc, cx);
       // First (or only) polyhedron: sub-tetrahedra (a, a+1, a+2, a+3), summed
       // in order straight into the scratch slots.
       for (int st = 0; st < nsub; st++) {
@@ -1063,13 +1157,20 @@ using namespace pgw;
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Frequency-independent part of the workspace: k → slot lists (CSR) and the
+// per-item class and sorted order.
+static size_t lists_bytes(int nkp, int ntet, long long items) {
+  return align256(sizeof(int) * (size_t)(nkp + 1)) + align256(sizeof(int) * (size_t)nkp) +
+         align256(sizeof(int) * (size_t)4 * ntet) + align256((size_t)items) + align256(sizeof(int) * (size_t)items) +
+         2 * align256(sizeof(unsigned) * NCLASS);
+}
+
 extern "C" size_t pg_bz_calcqdepw_par2_workspace(int nbnd, int nkp, int ncg, int nomx, int numin, int nom, int ntet,
                                                   int nom_chunk) {
   const long long nb1 = ncg + nomx + 1, nb2 = nbnd - ncg - numin;
   if (nb1 <= 0 || nb2 <= 0 || nkp <= 0 || ntet <= 0 || nom <= 0) return 0;
   const int nomc = (nom_chunk > 0 && nom_chunk < nom) ? nom_chunk : nom;
-  size_t b = align256(sizeof(int) * (size_t)(nkp + 1)) + align256(sizeof(int) * (size_t)nkp) +
-             align256(sizeof(int) * (size_t)4 * ntet);
+  size_t b = lists_bytes(nkp, ntet, nb1 * nb2 * ntet);
   b += align256(sizeof(double) * (size_t)4 * ntet * nomc * nb1 * nb2);
   return b;
 }
@@ -1082,6 +1183,8 @@ extern "C" int pg_bz_calcqdepw_par2(const double* enk, int nbnd, int nkp, double
   if (!enk || !kqid || !omega || !tetc || !kcw || !work) return PG_EARG;
   if (nb1 <= 0 || nb2 <= 0 || nkp <= 0 || ntet <= 0 || nom <= 0 || ncg < 0 || numin < 0) return PG_EARG;
   if (ntet != 6 * nkp) return PG_EARG;   // tetln = 6*kqid(ik)+it needs six tetrahedra per point
+  const long long items = (long long)nb1 * nb2 * ntet;
+  if (items >= (1ll << 31)) return PG_ETOOBIG;   // item indices are int
   int nomc = (nom_chunk > 0 && nom_chunk < nom) ? nom_chunk : nom;
   if (work_bytes < pg_bz_calcqdepw_par2_workspace(nbnd, nkp, ncg, nomx, numin, nom, ntet, nomc)) return PG_EWORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
@@ -1089,21 +1192,31 @@ extern "C" int pg_bz_calcqdepw_par2(const double* enk, int nbnd, int nkp, double
   int* kptr = (int*)w; w += align256(sizeof(int) * (size_t)(nkp + 1));
   int* kcount = (int*)w; w += align256(sizeof(int) * (size_t)nkp);
   int* kslot = (int*)w; w += align256(sizeof(int) * (size_t)4 * ntet);
+  unsigned char* cls = (unsigned char*)w; w += align256((size_t)items);
+  int* order = (int*)w; w += align256(sizeof(int) * (size_t)items);
+  unsigned* hist = (unsigned*)w; w += align256(sizeof(unsigned) * NCLASS);
+  unsigned* cursor = (unsigned*)w; w += align256(sizeof(unsigned) * NCLASS);
   double* scratch = (double*)w;
   k_kcsr_count<<<(nkp + 127) / 128, 128, 0, s>>>(tetc, ntet, nkp, kcount);
   k_kcsr_scan<<<1, 1, 0, s>>>(kcount, nkp, kptr);
   k_kcsr_fill<<<(nkp + 127) / 128, 128, 0, s>>>(tetc, ntet, nkp, kptr, kslot);
-  pg_count_launches(3);
   const int P = nb1 * nb2;
   const double wtet = 1.0 / ntet;
+  Params p;
+  p.enk = enk; p.kqid = kqid; p.omega = omega; p.tetc = tetc; p.scratch = scratch; p.order = nullptr;
+  p.status = d_status; p.counters = d_counters; p.ef = ef;
+  p.nbnd = nbnd; p.nkp = nkp; p.ncg = ncg; p.numin = numin; p.nb1 = nb1; p.nb2 = nb2; p.ntet = ntet;
+  p.om0 = 0; p.nomc = nomc;
+  // Sort the items by polyhedron class (frequency-independent, once per call).
+  const unsigned nblk = (unsigned)((items + 127) / 128);
+  if (cudaMemsetAsync(hist, 0, sizeof(unsigned) * NCLASS, s) != cudaSuccess) return PG_ECUDA;
+  k_tet_classify<<<nblk, 128, 0, s>>>(p, items, cls, hist);
+  k_class_offsets<<<1, 32, 0, s>>>(hist, cursor);
+  k_class_scatter<<<nblk, 128, 0, s>>>(cls, items, cursor, order);
+  pg_count_launches(6);
+  p.order = order;
   for (int om0 = 0; om0 < nom; om0 += nomc) {
-    Params p;
-    p.enk = enk; p.kqid = kqid; p.omega = omega; p.tetc = tetc; p.scratch = scratch;
-    p.status = d_status; p.counters = d_counters; p.ef = ef;
-    p.nbnd = nbnd; p.nkp = nkp; p.ncg = ncg; p.numin = numin; p.nb1 = nb1; p.nb2 = nb2; p.ntet = ntet;
     p.om0 = om0; p.nomc = (om0 + nomc <= nom) ? nomc : (nom - om0);
-    const long long items = (long long)P * ntet;
-    const unsigned nblk = (unsigned)((items + 127) / 128);
     k_tet_weights<<<nblk, 128, 0, s>>>(p);
     dim3 g((P + 127) / 128, nkp, p.nomc);
     k_gather<<<g, 128, 0, s>>>(scratch, kptr, kslot, P, nkp, p.nomc, om0, wtet, kcw);
@@ -1151,9 +1264,8 @@ extern "C" int pg_bz_calcqdepw_par2_noalloc(const double* enk, int nbnd, int nkp
   if (!enk || !kqid || !omega || !tetc || !kcw) return PG_EARG;
   if (nb1 <= 0 || nb2 <= 0 || nkp <= 0 || ntet <= 0 || nom <= 0 || ncg < 0 || numin < 0) return PG_EARG;
   if (ntet != 6 * nkp) return PG_EARG;
-  // Largest frequency chunk whose scratch fits next to the k lists.
-  const size_t lists = align256(sizeof(int) * (size_t)(nkp + 1)) + align256(sizeof(int) * (size_t)nkp) +
-                       align256(sizeof(int) * (size_t)4 * ntet);
+  // Largest frequency chunk whose scratch fits next to the k lists and the item order.
+  const size_t lists = lists_bytes(nkp, ntet, (long long)nb1 * nb2 * ntet);
   const size_t per_omega = sizeof(double) * (size_t)4 * ntet * (size_t)nb1 * nb2;
   if (lists + per_omega + 256 > (size_t)PG_NOALLOC_SCRATCH_BYTES) return PG_ETOOBIG;
   const size_t fit = ((size_t)PG_NOALLOC_SCRATCH_BYTES - lists - 256) / per_omega;
