@@ -63,6 +63,13 @@ constexpr int NTHREADS = 32 * (2 + NEPI);         // 320
 constexpr uint32_t TMEM_COLS = 512;               // two 256-column low accumulators
 constexpr unsigned long long WAIT_NS = 5000000000ull;   // 5 s per wait
 
+// Digit arrays are K-block major: plane (digit s, or frequency·S + digit for
+// B), 64-wide K-block, row, 64 values — one 128-row TMA tile is 16 KB of
+// contiguous memory (one page, whole DRAM bursts).
+__host__ __device__ __forceinline__ size_t digit_index(int plane, int r, long long k, int R_pad, int nkb) {
+  return (((size_t)plane * nkb + (size_t)(k >> 6)) * R_pad + r) * 64 + (size_t)(k & 63);
+}
+
 struct OzParams {
   double* out;          // [nsplit][wb][npair][128 (col)][128 (row)]
   unsigned* status;
@@ -116,21 +123,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
     }
   }
 }
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
-          smem_u32(dst)),
-      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::
+          "r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
       : "memory");
 }
 // The same tile written at this shared-memory offset in every CTA of `mask`,
 // completing bytes on the barrier at the same offset in each of them.
-__device__ __forceinline__ void tma_load_2d_mc(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y,
+__device__ __forceinline__ void tma_load_3d_mc(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z,
                                                uint16_t mask) {
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1, {%3, "
-      "%4}], [%2], %5;" ::"r"(smem_u32(dst)),
-      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y), "h"(mask)
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1, {%3, "
+      "%4, %5}], [%2], %6;" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z), "h"(mask)
       : "memory");
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -211,6 +218,22 @@ __host__ __device__ __forceinline__ void tri_pair(int lin, int n, int& i, int& j
   i = t; j = t + rem;
 }
 
+// Coordinates of load i of a CTA: digit pair (s, t) in the order d = 0..4,
+// s = 0..d, then the K-block; ya / yb = rows of the A tile and of this CTA's
+// half of the B tile, za / zb = their (plane, K-block) slices.
+__device__ __forceinline__ void load_coords(const OzParams& p, int i, int nkbs, int kb0, int ti, int wl, int cb,
+                                            int crank, int& ya, int& za, int& yb, int& zb) {
+  const int pi = i / nkbs;
+  int d = 0;
+  while ((d + 1) * (d + 2) / 2 <= pi) d++;
+  const int s_ = pi - d * (d + 1) / 2, t_ = d - s_;
+  const int kb = kb0 + (i - pi * nkbs);
+  ya = ti * TM;
+  za = s_ * p.nkb + kb;
+  yb = cb * TN + crank * TM;
+  zb = (wl * S + t_) * p.nkb + kb;
+}
+
 // ------------------------------------------------------ the digit GEMM
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_ozaki_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p) {
@@ -265,24 +288,23 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
   if (warp == 0) {
     // ---------------------------------------------------------- TMA producer
+    // Load order: for d = 0..4, s = 0..d (t = d − s), K-blocks kb0..kb1−1.
     if (lane == 0 && kb1 > kb0) {
+      const int nkbs = kb1 - kb0;
+      const int total = (S * (S + 1) / 2) * nkbs;
       int it = 0;
       bool ok = true;
-      for (int d = 0; d < S && ok; d++)
-        for (int s = 0; s <= d && ok; s++) {
-          const int t = d - s;
-          const int ya = s * p.R_pad + ti * TM;
-          const int yb = (wl * S + t) * p.R_pad + cb * TN + crank * TM;
-          for (int kb = kb0; kb < kb1 && ok; kb++, it++) {
-            const int st = it % NST;
-            if (it >= NST) ok = mbar_wait(empty + st, ((it / NST) - 1) & 1, abort_flag, p.status);
-            if (!ok) break;
-            unsigned char* sa = smem + st * STAGE_BYTES;
-            mbar_expect_tx(full + st, STAGE_BYTES);
-            tma_load_2d(sa, &tmA, full + st, kb * KB, ya);
-            tma_load_2d_mc(sa + TILE_BYTES * (1 + crank), &tmB, full + st, kb * KB, yb, both);
-          }
-        }
+      for (; it < total && ok; it++) {
+        const int st = it % NST;
+        if (it >= NST) ok = mbar_wait(empty + st, ((it / NST) - 1) & 1, abort_flag, p.status);
+        if (!ok) break;
+        int ya, za, yb, zb;
+        load_coords(p, it, nkbs, kb0, ti, wl, cb, crank, ya, za, yb, zb);
+        unsigned char* sa = smem + st * STAGE_BYTES;
+        mbar_expect_tx(full + st, STAGE_BYTES);
+        tma_load_3d(sa, &tmA, full + st, 0, ya, za);
+        tma_load_3d_mc(sa + TILE_BYTES * (1 + crank), &tmB, full + st, 0, yb, zb, both);
+      }
       // drain: the last phase of every stage must have been read by both CTAs'
       // MMAs (so every load and every remote arrival on this CTA has landed)
       const int issued = it;
@@ -460,7 +482,7 @@ __global__ void k_row_exp_A(const float* tmax, int R, int R_pad, int nkb, int* e
   if (threadIdx.x == 0) eA[r] = row_exponent(sm[0]);
 }
 
-// A digits: adig[s][r][k] (bf16), K contiguous; computed exactly in FP64.
+// A digits (bf16, K-block major, see digit_index); computed exactly in FP64.
 __global__ void k_digits_A(const double2* __restrict__ minm, long long K, int N, int R_pad, long long K_pad,
                            const int* eA, __nv_bfloat16* adig) {
   __shared__ double2 tile[32][33];
@@ -484,7 +506,7 @@ __global__ void k_digits_A(const double2* __restrict__ minm, long long K, int N,
         const double t = y * 256.0;
         const double dg = rint(t);
         y = t - dg;
-        adig[((size_t)s * R_pad + r) * K_pad + k] = __float2bfloat16_rn((float)dg);
+        adig[digit_index(s, r, k, R_pad, (int)(K_pad >> 6))] = __float2bfloat16_rn((float)dg);
       }
     }
   }
@@ -537,9 +559,10 @@ __global__ void k_rowmax_B(const __nv_bfloat16* __restrict__ adig, const float2*
   float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
   if (in) {
     float a0[4], a1[4], a2[4];
-    ld_bf16x4(adig + ((size_t)0 * R_pad + r) * K_pad + k0, a0);
-    ld_bf16x4(adig + ((size_t)1 * R_pad + r) * K_pad + k0, a1);
-    ld_bf16x4(adig + ((size_t)2 * R_pad + r) * K_pad + k0, a2);
+    const int nkb = (int)(K_pad >> 6);
+    ld_bf16x4(adig + digit_index(0, r, k0, R_pad, nkb), a0);
+    ld_bf16x4(adig + digit_index(1, r, k0, R_pad, nkb), a1);
+    ld_bf16x4(adig + digit_index(2, r, k0, R_pad, nkb), a2);
 #pragma unroll
     for (int j = 0; j < 4; j++) v[j] = fabsf((a0[j] * 0x1p-8f + a1[j] * 0x1p-16f) + a2[j] * 0x1p-24f);
   }
@@ -591,7 +614,7 @@ __global__ void k_digits_B(const __nv_bfloat16* __restrict__ adig, const int* eA
   {
     float a[S][4];
 #pragma unroll
-    for (int s = 0; s < S; s++) ld_bf16x4(adig + ((size_t)s * R_pad + r) * K_pad + k0, a[s]);
+    for (int s = 0; s < S; s++) ld_bf16x4(adig + digit_index(s, r, k0, R_pad, (int)(K_pad >> 6)), a[s]);
 #pragma unroll
     for (int j = 0; j < 4; j++) {
       vhi[j] = ((a[0][j] * 0x1p-8f + a[1][j] * 0x1p-16f) + a[2][j] * 0x1p-24f);   // exact
@@ -621,7 +644,7 @@ __global__ void k_digits_B(const __nv_bfloat16* __restrict__ adig, const int* eA
       }
     }
 #pragma unroll
-    for (int s = 0; s < S; s++) st_bf16x4(bdig + (((size_t)wl * S + s) * R_pad + r) * K_pad + k0, dg[s]);
+    for (int s = 0; s < S; s++) st_bf16x4(bdig + digit_index(wl * S + s, r, k0, R_pad, (int)(K_pad >> 6)), dg[s]);
   }
 }
 
@@ -660,6 +683,41 @@ struct MixedLayout {
   size_t off_adig, off_bdig, off_tmax, off_wpair, off_rmax, off_eA, off_fB, off_out, total;
 };
 
+static size_t gemm_smem_bytes() { return (size_t)NST * STAGE_BYTES + 1024 + 256; }
+
+// CTAs of k_ozaki_gemm that run at once on the current device (cached per device).
+#include <mutex>
+static std::mutex g_cap_mutex;
+static int g_cap[64] = {0};
+static int gemm_cta_capacity() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 2 * 74;
+  std::lock_guard<std::mutex> lk(g_cap_mutex);
+  if (g_cap[dev]) return g_cap[dev];
+  int ncl = 0;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(CL, 1, 1);
+  cfg.blockDim = dim3(NTHREADS);
+  cfg.dynamicSmemBytes = gemm_smem_bytes();
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaFuncSetAttribute(k_ozaki_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes()) !=
+          cudaSuccess ||
+      cudaOccupancyMaxActiveClusters(&ncl, k_ozaki_gemm, &cfg) != cudaSuccess || ncl <= 0) {
+    cudaGetLastError();
+    int sms = 148;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    ncl = sms / CL;
+  }
+  g_cap[dev] = ncl * CL;
+  return g_cap[dev];
+}
+
 static MixedLayout mixed_layout(int nb1, int nb2, int nkp, int npb, int wb, int kb_split) {
   MixedLayout L;
   L.K = (long long)nkp * nb1 * nb2;
@@ -675,9 +733,26 @@ static MixedLayout mixed_layout(int nb1, int nb2, int nkp, int npb, int wb, int 
   L.npair = L.nT * (L.nT + 1) / 2;          // stored 128×128 tiles
   // Exact-range split: a group sum over one split stays below 2^35
   // (5 pairs · kb·64 · 129² < 2^35  →  kb ≤ 6452).
-  const int kb_max = (kb_split > 0 && kb_split < 6400) ? kb_split : 6400;
-  L.nsplit = (L.nkb + kb_max - 1) / kb_max;
+  if (kb_split > 0) {
+    const int kb_max = kb_split < 6400 ? kb_split : 6400;
+    L.nsplit = (L.nkb + kb_max - 1) / kb_max;
+  } else {
+    // Automatic: the fewest splits (≥ the exact-range minimum, ≥ 256 K-blocks
+    // each) whose CTA count fills the last wave of the device to ≥ 95 %.
+    const int cap = gemm_cta_capacity();
+    const int ns0 = (L.nkb + 6399) / 6400;
+    int best = ns0;
+    double best_eff = 0.0;
+    for (int ns = ns0; ns <= 4 * ns0 + 8 && (ns == ns0 || L.nkb / ns >= 256); ns++) {
+      const double waves = (double)CL * L.nitems * wb * ns / cap;
+      const double eff = waves / ceil(waves);
+      if (eff > best_eff + 0.01) { best = ns; best_eff = eff; }
+      if (eff >= 0.95) break;
+    }
+    L.nsplit = best;
+  }
   L.kb_per_split = (L.nkb + L.nsplit - 1) / L.nsplit;
+  L.nsplit = (L.nkb + L.kb_per_split - 1) / L.kb_per_split;   // no empty split
   L.wb = wb;
   size_t o = 0;
   L.off_adig = o; o += al256((size_t)S * L.R_pad * L.K_pad * 2);
@@ -705,14 +780,16 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
   return fn;
 }
 
-static bool make_map(CUtensorMap* m, void* base, long long cols, long long rows) {
+// 3-D map over a K-block-major digit array: {64 values, R_pad rows, planes·nkb
+// K-blocks}; box 64 × 128 × 1 with the 128-byte swizzle the MMA descriptors use.
+static bool make_map(CUtensorMap* m, void* base, int R_pad, long long nslices) {
   auto enc = get_encode();
   if (!enc) return false;
-  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
-  cuuint32_t box[2] = {(cuuint32_t)KB, (cuuint32_t)TM};
-  cuuint32_t es[2] = {1, 1};
-  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+  cuuint64_t dims[3] = {(cuuint64_t)KB, (cuuint64_t)R_pad, (cuuint64_t)nslices};
+  cuuint64_t strides[2] = {(cuuint64_t)KB * 2, (cuuint64_t)KB * 2 * R_pad};
+  cuuint32_t box[3] = {(cuuint32_t)KB, (cuuint32_t)TM, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
              CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -759,9 +836,9 @@ extern "C" int pg_chi0_mixed(const void* minm, int nkp, const double* kcw, int n
   pg_count_launches(3);
 
   CUtensorMap mapA, mapB;
-  if (!make_map(&mapA, adig, L.K_pad, (long long)S * L.R_pad)) return PG_ECUDA;
-  if (!make_map(&mapB, bdig, L.K_pad, (long long)wb * S * L.R_pad)) return PG_ECUDA;
-  const size_t smem = (size_t)NST * STAGE_BYTES + 1024 + 256;
+  if (!make_map(&mapA, adig, L.R_pad, (long long)S * L.nkb)) return PG_ECUDA;
+  if (!make_map(&mapB, bdig, L.R_pad, (long long)wb * S * L.nkb)) return PG_ECUDA;
+  const size_t smem = gemm_smem_bytes();
   if (cudaFuncSetAttribute(k_ozaki_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return PG_ECUDA;
   OzParams op;

@@ -64,8 +64,10 @@ def test_digit_gemm_is_exact_white_box():
         n = int(np.prod(shape)) * np.dtype(dtype).itemsize
         return raw[offs[i]:offs[i] + n].view(dtype).reshape(shape)
 
-    A = _bf16(view(0, np.uint16, (S, R_pad, K_pad)))
-    B = _bf16(view(1, np.uint16, (wb, S, R_pad, K_pad)))[0]     # last batch: frequency nom-1 in slot 0
+    # digit arrays are K-block major: [plane][K-block][row][64]
+    A = _bf16(view(0, np.uint16, (S, nkb, R_pad, 64)).transpose(0, 2, 1, 3).reshape(S, R_pad, K_pad))
+    B = _bf16(view(1, np.uint16, (wb, S, nkb, R_pad, 64)).transpose(0, 1, 3, 2, 4).reshape(wb, S, R_pad, K_pad))[0]
+    # (last batch: frequency nom-1 in slot 0)
     eA = view(5, np.int32, (R_pad,))
     fB = view(6, np.int32, (wb, R_pad))[0]
     out = view(7, np.float64, (nsplit, wb, npair, 128, 128))[:, 0]
