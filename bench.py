@@ -199,7 +199,9 @@ def gpu_step(inp, step, timers=None, stream=None, precision="fp64", phases=None)
         peps.chi0_finalize(eps, inp.w.npb, inp.w.nom, stream=stream)
     if ev:
         ev[2].record(cs)
-    res = peps.eps_inverse(eps, inp.w.npb, inp.w.nom, stream=stream)
+    res = peps.eps_inverse(eps, inp.w.npb, inp.w.nom, stream=stream, precision=precision)
+    if precision == "mixed":
+        inp.statuses.append(res.status)
     if ev:
         ev[3].record(cs)
         phases.append(ev)
@@ -228,7 +230,7 @@ def fp64_gpu_estimate(inp, nk):
     _lib.check(rc, "pg_chi0_accumulate_f64")
     peps.chi0_finalize(eps, inp.w.npb, inp.w.nom)
     ev[2].record(cs)
-    peps.eps_inverse(eps, inp.w.npb, inp.w.nom)
+    peps.eps_inverse(eps, inp.w.npb, inp.w.nom, precision="fp64")
     ev[3].record(cs)
     torch.cuda.synchronize()
     t_w = ev[0].elapsed_time(ev[1]) * 1e-3

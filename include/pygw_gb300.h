@@ -113,6 +113,19 @@ size_t pg_eps_inverse_f64_workspace(int npb, int nom);
 int pg_eps_inverse_f64(void* eps, int npb, int nom, void* epsw1, void* epsw2, void* head, void* work,
                        size_t work_bytes, void* stream);
 
+/* ------------------------------------------- ε and ε⁻¹, mixed precision
+ * Same contract as pg_eps_inverse_f64 (pygw.py:3229-3271).  The inverse is
+ * computed in FP32 (complex Gauss–Jordan, partial pivoting) and refined
+ * `iters` times (0, 1 or 2) by X ← X + X·(I − A·X) with the residual formed on
+ * the tensor cores from six 8-bit digits per value (≈ 2^-48 relative to the
+ * row scales) and the sum in FP64; the q = 0 head/wings update stays FP64.
+ * omega_batch frequencies are inverted together (0 = all of them; the
+ * workspace grows with it).  d_status receives PG_ERR_TIMEOUT if a pipeline
+ * wait of the tensor-core kernel expired. */
+size_t pg_eps_inverse_mixed_workspace(int npb, int nom, int omega_batch);
+int pg_eps_inverse_mixed(void* eps, int npb, int nom, void* epsw1, void* epsw2, void* head, void* work,
+                         size_t work_bytes, int omega_batch, int iters, unsigned* d_status, void* stream);
+
 /* ------------------------------------------------------------ bookkeeping
  * Number of kernels this library has enqueued since it was loaded (all entry
  * points, all streams).  No counterpart in the reference. */

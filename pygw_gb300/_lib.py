@@ -31,6 +31,9 @@ SIGNATURES = {
     "pg_chi0_mixed_workspace": (c_size_t, [c_int, c_int, c_int, c_int, c_int, c_int]),
     "pg_chi0_mixed": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_int, c_double, c_void_p, c_void_p,
                               c_size_t, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    "pg_eps_inverse_mixed_workspace": (c_size_t, [c_int, c_int, c_int]),
+    "pg_eps_inverse_mixed": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_int,
+                                     c_int, c_void_p, c_void_p]),
     "pg_chi0_mixed_layout": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
     "pg_wings_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_int, c_int, c_int, c_double,
                              c_void_p, c_void_p, c_void_p]),

@@ -26,6 +26,7 @@ SOURCES = {
     "eps_f64.cu": [],
     "launches.cu": [],
     "chi0_mixed.cu": [],
+    "eps_mixed.cu": [],
 }
 
 

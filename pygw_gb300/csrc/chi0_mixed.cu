@@ -46,10 +46,11 @@
 #include <string.h>
 #include "pygw_status.h"
 #include "launches.h"
+#include "ozaki.h"
 
 namespace pgm {
 
-constexpr int S = 5;            // digits per value
+constexpr int S = OZ_S;         // digits per value
 constexpr int TM = 128;         // tile rows (A) = B rows loaded by one CTA
 constexpr int TN = 256;         // columns of a cluster's block
 constexpr int KB = 64;          // K per stage (one 128-byte swizzle row of bf16)
@@ -63,17 +64,14 @@ constexpr int NTHREADS = 32 * (2 + NEPI);         // 320
 constexpr uint32_t TMEM_COLS = 512;               // two 256-column low accumulators
 constexpr unsigned long long WAIT_NS = 5000000000ull;   // 5 s per wait
 
-// Digit arrays are K-block major: plane (digit s, or frequency·S + digit for
-// B), 64-wide K-block, row, 64 values — one 128-row TMA tile is 16 KB of
-// contiguous memory (one page, whole DRAM bursts).
-__host__ __device__ __forceinline__ size_t digit_index(int plane, int r, long long k, int R_pad, int nkb) {
-  return (((size_t)plane * nkb + (size_t)(k >> 6)) * R_pad + r) * 64 + (size_t)(k & 63);
-}
-
 struct OzParams {
   double* out;          // [nsplit][wb][npair][128 (col)][128 (row)]
   unsigned* status;
   int R_pad, nT, nTv, nC, npair, nkb, kb_per_split, nsplit, wb;
+  // general (full, non-symmetric) product: A digits per frequency, B with its own rows
+  int gen;              // 0: upper block triangle of V·diag(w)·Vᵀ; 1: full A·Bᵀ
+  int a_per_w;          // A planes per frequency (1) or shared by the batch (0)
+  int nTb, nTbv, nCb;   // B: 128-row tiles, tiles with real rows, 256-row blocks
 };
 
 // ------------------------------------------------------------ PTX helpers
@@ -218,9 +216,10 @@ __host__ __device__ __forceinline__ void tri_pair(int lin, int n, int& i, int& j
   i = t; j = t + rem;
 }
 
-// Coordinates of load i of a CTA: digit pair (s, t) in the order d = 0..4,
+// Coordinates of load i of a CTA: digit pair (s, t) in the order d = 0..SD−1,
 // s = 0..d, then the K-block; ya / yb = rows of the A tile and of this CTA's
 // half of the B tile, za / zb = their (plane, K-block) slices.
+template <int SD>
 __device__ __forceinline__ void load_coords(const OzParams& p, int i, int nkbs, int kb0, int ti, int wl, int cb,
                                             int crank, int& ya, int& za, int& yb, int& zb) {
   const int pi = i / nkbs;
@@ -229,12 +228,15 @@ __device__ __forceinline__ void load_coords(const OzParams& p, int i, int nkbs, 
   const int s_ = pi - d * (d + 1) / 2, t_ = d - s_;
   const int kb = kb0 + (i - pi * nkbs);
   ya = ti * TM;
-  za = s_ * p.nkb + kb;
+  za = ((p.a_per_w ? wl * SD : 0) + s_) * p.nkb + kb;
   yb = cb * TN + crank * TM;
-  zb = (wl * S + t_) * p.nkb + kb;
+  zb = (wl * SD + t_) * p.nkb + kb;
 }
 
 // ------------------------------------------------------ the digit GEMM
+// SD digits per value; digit pairs s + t ≤ SD − 1 (SD = 5 for χ0, 6 for the
+// residual of the ε⁻¹ refinement).
+template <int SD>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_ozaki_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -251,12 +253,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int crank = (int)cluster_rank();
   int rp, cb;
-  tri_pair(blockIdx.x / CL, p.nC, rp, cb);
+  if (p.gen) {
+    rp = (blockIdx.x / CL) / p.nCb;
+    cb = (blockIdx.x / CL) % p.nCb;
+  } else {
+    tri_pair(blockIdx.x / CL, p.nC, rp, cb);
+  }
   const int ti = 2 * rp + crank;                 // this CTA's 128-row tile
-  // column tiles 2cb, 2cb+1 of the block that lie in the upper triangle and
-  // hold real rows (at least one is computed, so both CTAs issue MMAs)
-  const int n_off = (ti > 2 * cb) ? 1 : 0;
-  int n_tiles = min(2 * cb + 2, p.nTv) - (2 * cb + n_off);
+  // column tiles 2cb, 2cb+1 of the block that are kept (upper triangle in the
+  // symmetric product) and hold real rows (at least one is computed, so both
+  // CTAs issue MMAs)
+  const int n_off = (!p.gen && ti > 2 * cb) ? 1 : 0;
+  int n_tiles = min(2 * cb + 2, p.nTbv) - (2 * cb + n_off);
   if (n_tiles < 1) n_tiles = 1;
   const int wl = blockIdx.y;        // frequency within the batch
   const int split = blockIdx.z;
@@ -288,10 +296,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
   if (warp == 0) {
     // ---------------------------------------------------------- TMA producer
-    // Load order: for d = 0..4, s = 0..d (t = d − s), K-blocks kb0..kb1−1.
+    // Load order: for d = 0..SD−1, s = 0..d (t = d − s), K-blocks kb0..kb1−1.
     if (lane == 0 && kb1 > kb0) {
       const int nkbs = kb1 - kb0;
-      const int total = (S * (S + 1) / 2) * nkbs;
+      const int total = (SD * (SD + 1) / 2) * nkbs;
       int it = 0;
       bool ok = true;
       for (; it < total && ok; it++) {
@@ -299,7 +307,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (it >= NST) ok = mbar_wait(empty + st, ((it / NST) - 1) & 1, abort_flag, p.status);
         if (!ok) break;
         int ya, za, yb, zb;
-        load_coords(p, it, nkbs, kb0, ti, wl, cb, crank, ya, za, yb, zb);
+        load_coords<SD>(p, it, nkbs, kb0, ti, wl, cb, crank, ya, za, yb, zb);
         unsigned char* sa = smem + st * STAGE_BYTES;
         mbar_expect_tx(full + st, STAGE_BYTES);
         tma_load_3d(sa, &tmA, full + st, 0, ya, za);
@@ -320,7 +328,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const uint32_t idesc = idesc_m128(TM * n_tiles);
       int it = 0, c = 0;
       bool ok = true;
-      for (int d = 0; d < S && ok; d++) {
+      for (int d = 0; d < SD && ok; d++) {
         if (d > 0) ok = mbar_wait(group_done, (d - 1) & 1, abort_flag, p.status);
         if (!ok) break;
         bool used[2] = {false, false};
@@ -364,15 +372,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int row = q * 32 + lane;                 // accumulator row (A tile row)
     const int tj = 2 * cb + h;
     const bool active = h >= n_off && h < n_off + n_tiles;
-    const bool stored = tj >= ti;                  // tile (ti, tj) is kept (upper triangle)
+    const bool stored = p.gen || tj >= ti;         // tile (ti, tj) is kept
     const uint32_t t_b0 = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * TM);
     const uint32_t t_b1 = t_b0 + TN;
-    const int pair = stored ? ti * p.nT - ti * (ti - 1) / 2 + (tj - ti) : 0;
+    const int pair = p.gen ? ti * p.nTb + tj : stored ? ti * p.nT - ti * (ti - 1) / 2 + (tj - ti) : 0;
     double* out = p.out + ((((size_t)split * p.wb + wl) * p.npair + pair) * TM) * TM;
     float hi[TM];                                  // high accumulator: multiples of 2^12, exact below 2^36
     int c = 0;
     bool ok = kb1 > kb0;
-    for (int d = 0; d < S && ok; d++) {
+    for (int d = 0; d < SD && ok; d++) {
 #pragma unroll
       for (int i = 0; i < TM; i++) hi[i] = 0.0f;
       const int nchunks_group = (d + 1) * nchunk_per_pass;
@@ -456,15 +464,6 @@ __global__ void k_block_max(const double2* __restrict__ minm, long long K, int N
   // round up so the float bound is never below the double value
   tmax[(size_t)I * nkb + kb] = __double2float_ru(mr);
   tmax[(size_t)(N + I) * nkb + kb] = __double2float_ru(mi);
-}
-
-// Row exponent e with max|x|·(1+2^-20) < 2^(e−1): every value of the row is then
-// |x / 2^e| < 1/2 and its leading digit |rint(256·x/2^e)| ≤ 128.
-__device__ __forceinline__ int row_exponent(float bound) {
-  if (!(bound > 0.0f)) return 0;
-  int e;
-  frexpf(bound * 1.000001f, &e);   // bound·(1+eps) in [2^(e−1), 2^e)
-  return e + 1;
 }
 
 __global__ void k_row_exp_A(const float* tmax, int R, int R_pad, int nkb, int* eA) {
@@ -706,9 +705,9 @@ static int gemm_cta_capacity() {
   cfg.dynamicSmemBytes = gemm_smem_bytes();
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (cudaFuncSetAttribute(k_ozaki_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes()) !=
+  if (cudaFuncSetAttribute(k_ozaki_gemm<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes()) !=
           cudaSuccess ||
-      cudaOccupancyMaxActiveClusters(&ncl, k_ozaki_gemm, &cfg) != cudaSuccess || ncl <= 0) {
+      cudaOccupancyMaxActiveClusters(&ncl, k_ozaki_gemm<S>, &cfg) != cudaSuccess || ncl <= 0) {
     cudaGetLastError();
     int sms = 148;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -839,10 +838,11 @@ extern "C" int pg_chi0_mixed(const void* minm, int nkp, const double* kcw, int n
   if (!make_map(&mapA, adig, L.R_pad, (long long)S * L.nkb)) return PG_ECUDA;
   if (!make_map(&mapB, bdig, L.R_pad, (long long)wb * S * L.nkb)) return PG_ECUDA;
   const size_t smem = gemm_smem_bytes();
-  if (cudaFuncSetAttribute(k_ozaki_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_ozaki_gemm<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return PG_ECUDA;
   OzParams op;
   op.out = out; op.status = d_status; op.R_pad = L.R_pad; op.nT = L.nT; op.nTv = L.nTv; op.nC = L.nC;
+  op.gen = 0; op.a_per_w = 0; op.nTb = L.nT; op.nTbv = L.nTv; op.nCb = L.nC;
   op.npair = L.npair; op.nkb = L.nkb; op.kb_per_split = L.kb_per_split; op.nsplit = L.nsplit; op.wb = wb;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -867,13 +867,50 @@ extern "C" int pg_chi0_mixed(const void* minm, int nkp, const double* kcw, int n
     cfg.numAttrs = 1;
     const int batch = om0 / wb;
     if (gemm_events && cudaEventRecord((cudaEvent_t)gemm_events[2 * batch], s) != cudaSuccess) return PG_ECUDA;
-    if (cudaLaunchKernelEx(&cfg, k_ozaki_gemm, mapA, mapB, op) != cudaSuccess) return PG_ECUDA;
+    if (cudaLaunchKernelEx(&cfg, k_ozaki_gemm<S>, mapA, mapB, op) != cudaSuccess) return PG_ECUDA;
     if (gemm_events && cudaEventRecord((cudaEvent_t)gemm_events[2 * batch + 1], s) != cudaSuccess) return PG_ECUDA;
     k_assemble<<<dim3((npb + 127) / 128, npb, nw), 128, 0, s>>>(out, eA, fB, npb, L.R_pad, L.nT, L.npair, L.nsplit,
                                                                wb, om0, (double2*)eps);
     pg_count_launches(6);
   }
   return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ECUDA;
+}
+
+// Full product for the refinement of ε⁻¹ (see ozaki.h).
+int pgm::launch_gemm_general(const __nv_bfloat16* adig, const __nv_bfloat16* bdig, int sd, int R_padA, int R_padB,
+                             int nTbv, int nkb, int nw, double* out, unsigned* status, cudaStream_t s) {
+  // group sums stay below 2^35: sd pairs · nkb·64 · 129² < 2^35
+  if (R_padA <= 0 || R_padB <= 0 || R_padA % TN || R_padB % TN || nkb <= 0 || nw <= 0 || (sd != 5 && sd != 6) ||
+      (long long)sd * nkb * 64 * 16641 >= (1ll << 35))
+    return PG_EARG;
+  CUtensorMap mapA, mapB;
+  if (!make_map(&mapA, (void*)adig, R_padA, (long long)nw * sd * nkb)) return PG_ECUDA;
+  if (!make_map(&mapB, (void*)bdig, R_padB, (long long)nw * sd * nkb)) return PG_ECUDA;
+  const size_t smem = gemm_smem_bytes();
+  auto kern = (sd == 6) ? k_ozaki_gemm<6> : k_ozaki_gemm<5>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return PG_ECUDA;
+  OzParams op;
+  memset(&op, 0, sizeof(op));
+  op.out = out; op.status = status;
+  op.R_pad = R_padA; op.nT = R_padA / TM; op.nTv = R_padA / TM; op.nC = R_padA / TN;
+  op.gen = 1; op.a_per_w = 1; op.nTb = R_padB / TM; op.nTbv = nTbv; op.nCb = R_padB / TN;
+  op.npair = op.nT * op.nTb; op.nkb = nkb; op.kb_per_split = nkb; op.nsplit = 1; op.wb = nw;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(CL * op.nC * op.nCb), (unsigned)nw, 1);
+  cfg.blockDim = dim3(NTHREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, kern, mapA, mapB, op) != cudaSuccess) return PG_ECUDA;
+  pg_count_launches(1);
+  return PG_OK;
 }
 
 // Workspace layout of pg_chi0_mixed, for inspection by tests:

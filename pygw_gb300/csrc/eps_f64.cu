@@ -14,6 +14,7 @@
 #include <stdint.h>
 #include "pygw_status.h"
 #include "launches.h"
+#include "eps_internal.h"
 
 namespace pge {
 
@@ -214,6 +215,28 @@ __global__ void k_sub_identity(double2* eps, int N) {
   if (I < N) eps[(size_t)N * N * w + (size_t)I + (size_t)N * I].x -= 1.0;
 }
 
+void launch_sym_add_identity(double2* eps, int N, int nom, cudaStream_t s) {
+  const int TB = 128;
+  k_sym_add_identity<<<dim3((N + TB - 1) / TB, N, nom), TB, 0, s>>>(eps, N);
+  pg_count_launches(1);
+}
+
+void launch_finish(double2* eps, int N, int nom, double2* epsw1, double2* epsw2, double2* head, double2* bw1,
+                   double2* w2b, cudaStream_t s) {
+  const int TB = 128;
+  if (epsw1) {
+    dim3 gv((N + TB - 1) / TB, nom);
+    k_matvec<<<gv, TB, 0, s>>>(eps, N, epsw1, bw1, 0);
+    k_matvec<<<gv, TB, 0, s>>>(eps, N, epsw2, w2b, 1);
+    k_head_update<<<nom, 256, 0, s>>>(N, bw1, w2b, epsw1, epsw2, head);
+    k_head_rank1<<<dim3((N + TB - 1) / TB, N, nom), TB, 0, s>>>(eps, N, bw1, w2b, head);
+    k_head_minus_one<<<(nom + 127) / 128, 128, 0, s>>>(head, nom);
+    pg_count_launches(5);
+  }
+  k_sub_identity<<<dim3((N + TB - 1) / TB, nom), TB, 0, s>>>(eps, N);
+  pg_count_launches(1);
+}
+
 }  // namespace pge
 
 using namespace pge;
@@ -243,27 +266,14 @@ extern "C" int pg_eps_inverse_f64(void* eps_, int npb, int nom, void* epsw1_, vo
   double2* w2b = (double2*)wp;
   const int TB = 128;
   dim3 gsq((N + TB - 1) / TB, N, nom);
-  k_sym_add_identity<<<gsq, TB, 0, s>>>(eps, N);
+  launch_sym_add_identity(eps, N, nom, s);
   for (int k = 0; k < N; k++) {
     k_gj_pivot<<<nom, 256, 0, s>>>(eps, N, k, perm);
     k_gj_eliminate<<<gsq, TB, 0, s>>>(eps, N, k);
     k_gj_column<<<dim3((N + TB - 1) / TB, nom), TB, 0, s>>>(eps, N, k);
   }
   k_gj_unpermute<<<nom, 256, 0, s>>>(eps, N, perm);
-  pg_count_launches(2 + 3ull * N);
-  if (q0) {
-    double2* epsw1 = (double2*)epsw1_;
-    double2* epsw2 = (double2*)epsw2_;
-    double2* head = (double2*)head_;
-    dim3 gv((N + TB - 1) / TB, nom);
-    k_matvec<<<gv, TB, 0, s>>>(eps, N, epsw1, bw1, 0);
-    k_matvec<<<gv, TB, 0, s>>>(eps, N, epsw2, w2b, 1);
-    k_head_update<<<nom, 256, 0, s>>>(N, bw1, w2b, epsw1, epsw2, head);
-    k_head_rank1<<<gsq, TB, 0, s>>>(eps, N, bw1, w2b, head);
-    k_head_minus_one<<<(nom + 127) / 128, 128, 0, s>>>(head, nom);
-    pg_count_launches(5);
-  }
-  k_sub_identity<<<dim3((N + TB - 1) / TB, nom), TB, 0, s>>>(eps, N);
-  pg_count_launches(1);
+  pg_count_launches(1 + 3ull * N);
+  launch_finish(eps, N, nom, q0 ? (double2*)epsw1_ : nullptr, (double2*)epsw2_, (double2*)head_, bw1, w2b, s);
   return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ECUDA;
 }

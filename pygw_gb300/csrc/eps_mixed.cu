@@ -1,0 +1,431 @@
+// ε⁻¹ in mixed precision: FP32 Gauss–Jordan inverse, refined in FP64 with
+// the residual on the tensor cores.
+//
+// The ε block of calc_eps (pygw.py:3229-3271) inverts the Hermitian
+// A = (ε + εᴴ)/2 + I per frequency with scipy.linalg.inv in FP64.  Here:
+//   1. X0 = A⁻¹ in FP32 (complex Gauss–Jordan, partial pivoting by |Re|+|Im|,
+//      the same algorithm as the FP64 path);
+//   2. `iters` refinement steps  R = I − A·X (split-precision digit GEMM on
+//      tcgen05: A and X split into six 8-bit digits per value, digit pairs
+//      s + t ≤ 5 summed exactly, ≈ 2^-48 relative to the row scales),
+//      X ← X + X·R (FP32 product, FP64 sum: R is small, so FP32 suffices);
+//   3. the q → 0 head/wings update and −I in FP64 (shared with the FP64 path).
+// Each refinement step squares the relative error of X (‖I − X·A‖ < 1), so
+// one or two steps take the FP32 inverse (≈ κ·1e-7) to the FP64 level.
+//
+// Real form of the complex product C = A·X used by the digit GEMM:
+//   A_real (2N × 2N) = [[Re A, −Im A], [Im A, Re A]],  B (N × 2N): B[j] = [Re X(:,j); Im X(:,j)],
+//   G = A_real · Bᵀ,  C(i,j) = G[i][j] + i·G[N+i][j].
+// A is Hermitian, so row r of A is the conjugate of its column r and every
+// digit row is read from contiguous memory.
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include "pygw_status.h"
+#include "launches.h"
+#include "ozaki.h"
+#include "eps_internal.h"
+
+namespace pgx {
+
+using pgm::digit_index;
+using pgm::row_exponent;
+constexpr int S = 6;            // digits per value in the residual (≈ 2^-48 of the row scales)
+
+// ------------------------------------------------------------ FP32 inverse
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 crecipf(float2 a) {
+  // Smith's algorithm for 1/a.
+  if (fabsf(a.x) >= fabsf(a.y)) {
+    const float r = a.y / a.x, d = a.x + a.y * r;
+    return make_float2(1.0f / d, -r / d);
+  } else {
+    const float r = a.x / a.y, d = a.x * r + a.y;
+    return make_float2(r / d, -1.0f / d);
+  }
+}
+
+__global__ void k_to_f32(const double2* __restrict__ a, float2* __restrict__ x, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+
+// Pivot search, row swap and pivot-row scaling for step k (one block per ω).
+__global__ void k_gj32_pivot(float2* X, int N, int k, int* perm) {
+  const int w = blockIdx.x;
+  float2* E = X + (size_t)N * N * w;
+  __shared__ float sv[256];
+  __shared__ int si[256];
+  float best = -1.0f;
+  int bi = N;
+  for (int i = k + threadIdx.x; i < N; i += blockDim.x) {
+    const float2 a = E[(size_t)i + (size_t)N * k];
+    const float v = fabsf(a.x) + fabsf(a.y);
+    if (v > best) { best = v; bi = i; }
+  }
+  sv[threadIdx.x] = best;
+  si[threadIdx.x] = bi;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      const float v2 = sv[threadIdx.x + s];
+      const int i2 = si[threadIdx.x + s];
+      if (v2 > sv[threadIdx.x] || (v2 == sv[threadIdx.x] && i2 < si[threadIdx.x])) {
+        sv[threadIdx.x] = v2;
+        si[threadIdx.x] = i2;
+      }
+    }
+    __syncthreads();
+  }
+  const int p = (si[0] < N) ? si[0] : k;   // a column without a finite pivot keeps its row
+  if (threadIdx.x == 0) perm[(size_t)N * w + k] = p;
+  if (p != k) {
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+      const float2 t = E[(size_t)k + (size_t)N * j];
+      E[(size_t)k + (size_t)N * j] = E[(size_t)p + (size_t)N * j];
+      E[(size_t)p + (size_t)N * j] = t;
+    }
+  }
+  __syncthreads();
+  const float2 r = crecipf(E[(size_t)k + (size_t)N * k]);
+  __syncthreads();
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    if (j == k) E[(size_t)k + (size_t)N * k] = r;
+    else E[(size_t)k + (size_t)N * j] = cmulf(E[(size_t)k + (size_t)N * j], r);
+  }
+}
+
+// X[i,j] −= X[i,k]·X[k,j] for i ≠ k, j ≠ k.
+__global__ void k_gj32_eliminate(float2* X, int N, int k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  const int w = blockIdx.z;
+  if (i >= N || i == k || j == k) return;
+  float2* E = X + (size_t)N * N * w;
+  const float2 f = E[(size_t)i + (size_t)N * k];
+  const float2 a = E[(size_t)k + (size_t)N * j];
+  float2& d = E[(size_t)i + (size_t)N * j];
+  d.x -= f.x * a.x - f.y * a.y;
+  d.y -= f.x * a.y + f.y * a.x;
+}
+
+// X[i,k] ← −X[i,k]·X[k,k] for i ≠ k (X[k,k] already holds 1/pivot).
+__global__ void k_gj32_column(float2* X, int N, int k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int w = blockIdx.y;
+  if (i >= N || i == k) return;
+  float2* E = X + (size_t)N * N * w;
+  const float2 r = E[(size_t)k + (size_t)N * k];
+  const float2 v = cmulf(E[(size_t)i + (size_t)N * k], r);
+  E[(size_t)i + (size_t)N * k] = make_float2(-v.x, -v.y);
+}
+
+// Undo the row interchanges on the columns of the inverse (reverse order).
+__global__ void k_gj32_unpermute(float2* X, int N, const int* perm) {
+  const int w = blockIdx.x;
+  float2* E = X + (size_t)N * N * w;
+  for (int k = N - 1; k >= 0; k--) {
+    const int p = perm[(size_t)N * w + k];
+    if (p != k && p >= 0 && p < N) {
+      for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const float2 t = E[(size_t)i + (size_t)N * k];
+        E[(size_t)i + (size_t)N * k] = E[(size_t)i + (size_t)N * p];
+        E[(size_t)i + (size_t)N * p] = t;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ digits
+__device__ __forceinline__ double2 ld2(const double2* p) { return *p; }
+__device__ __forceinline__ double2 ld2(const float2* p) { const float2 v = *p; return make_double2(v.x, v.y); }
+
+// Exponent of column j of M (max over k of |Re|, |Im|) for row j of the real
+// form (and row N + j when two_rows).  Grid (N, nw), 256 threads.
+template <typename T>
+__global__ void k_col_exp(const T* M, int N, int R_pad, int two_rows, int* e) {
+  const int j = blockIdx.x, w = blockIdx.y;
+  const T* col = M + (size_t)N * N * w + (size_t)N * j;
+  double m = 0.0;
+  for (int k = threadIdx.x; k < N; k += blockDim.x) {
+    const double2 v = ld2(col + k);
+    m = fmax(m, fmax(fabs(v.x), fabs(v.y)));
+  }
+  __shared__ double sm[256];
+  sm[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const int ex = row_exponent(__double2float_ru(sm[0]));
+    e[(size_t)R_pad * w + j] = ex;
+    if (two_rows) e[(size_t)R_pad * w + N + j] = ex;
+  }
+}
+
+// S signed 8-bit digits of x relative to 2^e (exact FP64 arithmetic).
+__device__ __forceinline__ void digitsS(double x, int e, __nv_bfloat16 (&d)[S]) {
+  double y = ldexp(x, -e);
+#pragma unroll
+  for (int s = 0; s < S; s++) {
+    const double t = y * 256.0;
+    const double dg = rint(t);
+    y = t - dg;
+    d[s] = __float2bfloat16_rn((float)dg);
+  }
+}
+
+// A digits: rows r and N + r of A_real from column r of the Hermitian A.
+// Grid (ceil(N/256), N, nw).
+__global__ void k_digits_herm(const double2* __restrict__ A, int N, int R_pad, int nkb, const int* eA,
+                              __nv_bfloat16* adig) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y, w = blockIdx.z;
+  if (k >= N) return;
+  const double2 x = A[(size_t)N * N * w + (size_t)N * r + k];   // A(k, r) = conj A(r, k)
+  const int e = eA[(size_t)R_pad * w + r];
+  __nv_bfloat16 dre[S], dim[S];
+  digitsS(x.x, e, dre);
+  digitsS(x.y, e, dim);
+#pragma unroll
+  for (int s = 0; s < S; s++) {
+    const int pl = w * S + s;
+    adig[digit_index(pl, r, k, R_pad, nkb)] = dre[s];                 //  Re A(r,k)
+    adig[digit_index(pl, r, N + k, R_pad, nkb)] = dim[s];             // −Im A(r,k)
+    adig[digit_index(pl, N + r, k, R_pad, nkb)] = __hneg(dim[s]);     //  Im A(r,k)
+    adig[digit_index(pl, N + r, N + k, R_pad, nkb)] = dre[s];         //  Re A(r,k)
+  }
+}
+
+// B digits: row j = [Re X(:, j); Im X(:, j)].  Grid (ceil(N/256), N, nw).
+template <typename T>
+__global__ void k_digits_cols(const T* __restrict__ X, int N, int R_pad, int nkb, const int* fB, __nv_bfloat16* bdig) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y, w = blockIdx.z;
+  if (k >= N) return;
+  const double2 x = ld2(X + (size_t)N * N * w + (size_t)N * j + k);
+  const int e = fB[(size_t)R_pad * w + j];
+  __nv_bfloat16 dre[S], dim[S];
+  digitsS(x.x, e, dre);
+  digitsS(x.y, e, dim);
+#pragma unroll
+  for (int s = 0; s < S; s++) {
+    const int pl = w * S + s;
+    bdig[digit_index(pl, j, k, R_pad, nkb)] = dre[s];
+    bdig[digit_index(pl, j, N + k, R_pad, nkb)] = dim[s];
+  }
+}
+
+// R = I − A·X from the digit-GEMM tiles.  Grid (ceil(N/128), N, nw).
+__global__ void k_residual(const double* __restrict__ out, const int* eA, const int* fB, int N, int R_padA, int R_padB,
+                           int nTb, int ntile, double2* R) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y, w = blockIdx.z;
+  if (i >= N) return;
+  auto G = [&](int r, int c) -> double {
+    const int tile = (r >> 7) * nTb + (c >> 7);
+    const double v = out[((size_t)w * ntile + tile) * 16384 + (size_t)(c & 127) * 128 + (r & 127)];
+    return ldexp(v, eA[(size_t)R_padA * w + r] + fB[(size_t)R_padB * w + c] - 16);
+  };
+  const double re = G(i, j), im = G(N + i, j);
+  R[(size_t)N * N * w + (size_t)N * j + i] = make_double2((i == j ? 1.0 : 0.0) - re, -im);
+}
+
+// Xnew = X + X·R (complex, FP32 products and accumulation, FP64 sum with X).
+// 64×64 output tile per block, 16×16 threads with 4×4 outputs each.
+template <typename T>
+__global__ void __launch_bounds__(256) k_correct(const T* __restrict__ X, const double2* __restrict__ R, int N,
+                                                 double2* __restrict__ Xnew) {
+  __shared__ float2 sx[16][64];
+  __shared__ float2 sr[16][64];
+  const int w = blockIdx.z;
+  const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const T* Xw = X + (size_t)N * N * w;
+  const double2* Rw = R + (size_t)N * N * w;
+  float2 acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) acc[a][b] = make_float2(0.0f, 0.0f);
+  for (int k0 = 0; k0 < N; k0 += 16) {
+    for (int e = threadIdx.x; e < 1024; e += 256) {
+      const int ii = e & 63, kk = e >> 6;                 // X(i0+ii, k0+kk): 64 consecutive rows
+      const int i = i0 + ii, k = k0 + kk;
+      const double2 v = (i < N && k < N) ? ld2(Xw + (size_t)N * k + i) : make_double2(0.0, 0.0);
+      sx[kk][ii] = make_float2((float)v.x, (float)v.y);
+      const int kr = e & 15, jj = e >> 4;                 // R(k0+kr, j0+jj): 16 consecutive rows
+      const int k2 = k0 + kr, j = j0 + jj;
+      const double2 u = (k2 < N && j < N) ? Rw[(size_t)N * j + k2] : make_double2(0.0, 0.0);
+      sr[kr][jj] = make_float2((float)u.x, (float)u.y);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; kk++) {
+      float2 xa[4], rb[4];
+#pragma unroll
+      for (int a = 0; a < 4; a++) xa[a] = sx[kk][ty * 4 + a];
+#pragma unroll
+      for (int b = 0; b < 4; b++) rb[b] = sr[kk][tx * 4 + b];
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+          acc[a][b].x = fmaf(xa[a].x, rb[b].x, fmaf(-xa[a].y, rb[b].y, acc[a][b].x));
+          acc[a][b].y = fmaf(xa[a].x, rb[b].y, fmaf(xa[a].y, rb[b].x, acc[a][b].y));
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      const int i = i0 + ty * 4 + a, j = j0 + tx * 4 + b;
+      if (i < N && j < N) {
+        const double2 x = ld2(Xw + (size_t)N * j + i);
+        Xnew[(size_t)N * N * w + (size_t)N * j + i] = make_double2(x.x + (double)acc[a][b].x, x.y + (double)acc[a][b].y);
+      }
+    }
+}
+
+__global__ void k_to_f64(const float2* __restrict__ x, double2* __restrict__ a, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = make_double2((double)x[i].x, (double)x[i].y);
+}
+
+// ------------------------------------------------------------ workspace
+static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct Layout {
+  int N, nb, R_padA, R_padB, nkb, nTb, ntile;
+  long long K_pad;
+  size_t perm, x32, x64, res, adig, bdig, eA, fB, out, bw1, w2b, total;
+};
+
+static Layout layout(int N, int nom, int nb) {
+  Layout L;
+  L.N = N;
+  L.nb = nb;
+  L.R_padA = (2 * N + pgm::OZ_BLOCK - 1) / pgm::OZ_BLOCK * pgm::OZ_BLOCK;
+  L.R_padB = (N + pgm::OZ_BLOCK - 1) / pgm::OZ_BLOCK * pgm::OZ_BLOCK;
+  L.K_pad = (2LL * N + pgm::OZ_KB - 1) / pgm::OZ_KB * pgm::OZ_KB;
+  L.nkb = (int)(L.K_pad / pgm::OZ_KB);
+  L.nTb = L.R_padB / pgm::OZ_TILE;
+  L.ntile = (L.R_padA / pgm::OZ_TILE) * L.nTb;
+  const size_t NN = (size_t)N * N;
+  size_t o = 0;
+  L.perm = o; o += al256(sizeof(int) * (size_t)N * nb);
+  L.x32 = o; o += al256(sizeof(float2) * NN * nb);
+  L.x64 = o; o += al256(sizeof(double2) * NN * nb);
+  L.res = o; o += al256(sizeof(double2) * NN * nb);
+  L.adig = o; o += al256((size_t)2 * S * L.R_padA * L.K_pad * nb);
+  L.bdig = o; o += al256((size_t)2 * S * L.R_padB * L.K_pad * nb);
+  L.eA = o; o += al256(sizeof(int) * (size_t)L.R_padA * nb);
+  L.fB = o; o += al256(sizeof(int) * (size_t)L.R_padB * nb);
+  L.out = o; o += al256(sizeof(double) * (size_t)L.ntile * 16384 * nb);
+  L.bw1 = o; o += al256(sizeof(double2) * (size_t)N * nom);
+  L.w2b = o; o += al256(sizeof(double2) * (size_t)N * nom);
+  L.total = o;
+  return L;
+}
+
+// One refinement step: dst = X + X·(I − A·X) for the nw frequencies of a batch
+// (A's digits and exponents are already in the workspace; dst ≠ X).
+template <typename T>
+static int refine_step(const T* X, double2* dst, const Layout& L, char* w, int nw, unsigned* status, cudaStream_t s) {
+  const int N = L.N;
+  int* fB = (int*)(w + L.fB);
+  __nv_bfloat16* bdig = (__nv_bfloat16*)(w + L.bdig);
+  if (cudaMemsetAsync(fB, 0, sizeof(int) * (size_t)L.R_padB * nw, s) != cudaSuccess) return PG_ECUDA;
+  if (cudaMemsetAsync(bdig, 0, (size_t)2 * S * L.R_padB * L.K_pad * nw, s) != cudaSuccess) return PG_ECUDA;
+  k_col_exp<T><<<dim3(N, nw), 256, 0, s>>>(X, N, L.R_padB, 0, fB);
+  k_digits_cols<T><<<dim3((N + 255) / 256, N, nw), 256, 0, s>>>(X, N, L.R_padB, L.nkb, fB, bdig);
+  pg_count_launches(2);
+  double* out = (double*)(w + L.out);
+  const int rc = pgm::launch_gemm_general((const __nv_bfloat16*)(w + L.adig), bdig, S, L.R_padA, L.R_padB,
+                                          (N + pgm::OZ_TILE - 1) / pgm::OZ_TILE, L.nkb, nw, out, status, s);
+  if (rc != PG_OK) return rc;
+  double2* R = (double2*)(w + L.res);
+  k_residual<<<dim3((N + 127) / 128, N, nw), 128, 0, s>>>(out, (const int*)(w + L.eA), fB, N, L.R_padA, L.R_padB,
+                                                         L.nTb, L.ntile, R);
+  k_correct<T><<<dim3((N + 63) / 64, (N + 63) / 64, nw), 256, 0, s>>>(X, R, N, dst);
+  pg_count_launches(2);
+  return PG_OK;
+}
+
+}  // namespace pgx
+
+using namespace pgx;
+
+extern "C" size_t pg_eps_inverse_mixed_workspace(int npb, int nom, int omega_batch) {
+  if (npb <= 0 || nom <= 0) return 0;
+  const int nb = (omega_batch > 0 && omega_batch < nom) ? omega_batch : nom;
+  return layout(npb, nom, nb).total;
+}
+
+// eps: the χ0 part (as for pg_eps_inverse_f64); on return ε⁻¹ − 1.
+// omega_batch frequencies are inverted together (0 = all); iters (0, 1 or 2)
+// refinement steps follow the FP32 inverse (0 = the FP32 inverse alone).
+extern "C" int pg_eps_inverse_mixed(void* eps_, int npb, int nom, void* epsw1_, void* epsw2_, void* head_, void* work,
+                                    size_t work_bytes, int omega_batch, int iters, unsigned* d_status, void* stream) {
+  if (!eps_ || npb <= 0 || nom <= 0 || !work || iters < 0 || iters > 2) return PG_EARG;
+  const bool q0 = epsw1_ != nullptr;
+  if (q0 && (!epsw2_ || !head_)) return PG_EARG;
+  const int nb = (omega_batch > 0 && omega_batch < nom) ? omega_batch : nom;
+  const Layout L = layout(npb, nom, nb);
+  if (work_bytes < L.total) return PG_EWORKSPACE;
+  if ((long long)S * L.nkb * 64 * 16641 >= (1ll << 35)) return PG_ETOOBIG;
+  cudaStream_t s = (cudaStream_t)stream;
+  double2* eps = (double2*)eps_;
+  const int N = npb;
+  const size_t NN = (size_t)N * N;
+  char* w = (char*)work;
+  int* perm = (int*)(w + L.perm);
+  float2* x32 = (float2*)(w + L.x32);
+  double2* x64 = (double2*)(w + L.x64);
+  int* eA = (int*)(w + L.eA);
+  __nv_bfloat16* adig = (__nv_bfloat16*)(w + L.adig);
+  const int TB = 128;
+  pge::launch_sym_add_identity(eps, N, nom, s);
+  for (int w0 = 0; w0 < nom; w0 += nb) {
+    const int nw = (w0 + nb <= nom) ? nb : nom - w0;
+    double2* A = eps + NN * w0;
+    const size_t n = NN * nw;
+    k_to_f32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A, x32, n);
+    dim3 gsq((N + TB - 1) / TB, N, nw);
+    for (int k = 0; k < N; k++) {
+      k_gj32_pivot<<<nw, 256, 0, s>>>(x32, N, k, perm);
+      k_gj32_eliminate<<<gsq, TB, 0, s>>>(x32, N, k);
+      k_gj32_column<<<dim3((N + TB - 1) / TB, nw), TB, 0, s>>>(x32, N, k);
+    }
+    k_gj32_unpermute<<<nw, 256, 0, s>>>(x32, N, perm);
+    pg_count_launches(2 + 3ull * N);
+    if (iters == 0) {
+      k_to_f64<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x32, A, n);
+      pg_count_launches(1);
+      continue;
+    }
+    // digits of A (shared by the refinement steps of this batch)
+    if (cudaMemsetAsync(eA, 0, sizeof(int) * (size_t)L.R_padA * nw, s) != cudaSuccess) return PG_ECUDA;
+    if (cudaMemsetAsync(adig, 0, (size_t)2 * S * L.R_padA * L.K_pad * nw, s) != cudaSuccess) return PG_ECUDA;
+    k_col_exp<double2><<<dim3(N, nw), 256, 0, s>>>(A, N, L.R_padA, 1, eA);
+    k_digits_herm<<<dim3((N + 255) / 256, N, nw), 256, 0, s>>>(A, N, L.R_padA, L.nkb, eA, adig);
+    pg_count_launches(2);
+    for (int it = 0; it < iters; it++) {
+      // the last step writes the result over A (no longer needed once its residual is formed)
+      double2* dst = (it == iters - 1) ? A : x64;
+      const int rc = (it == 0) ? refine_step<float2>(x32, dst, L, w, nw, d_status, s)
+                               : refine_step<double2>(x64, dst, L, w, nw, d_status, s);
+      if (rc != PG_OK) return rc;
+    }
+  }
+  pge::launch_finish(eps, N, nom, q0 ? (double2*)epsw1_ : nullptr, (double2*)epsw2_, (double2*)head_,
+                     (double2*)(w + L.bw1), (double2*)(w + L.w2b), s);
+  return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ECUDA;
+}

@@ -236,21 +236,57 @@ def chi0_finalize(eps, npb, nom, stream=None, precision=None):
     return eps
 
 
-def eps_inverse(eps, npb, nom, epsw1=None, head=None, stream=None, precision=None, work=None):
-    """ε⁻¹ − 1 in place; for q = 0 also the updated wings and head."""
+REFINE_ITERS = 2       # refinement steps of the mixed-precision inverse (0 = FP32 inverse alone)
+
+
+def eps_inverse_batch(npb, nom, budget_bytes=None):
+    """Frequencies per batch of the mixed-precision inverse, sized to a memory
+    budget (default: 30 % of the free device memory)."""
     lib = _lib.load()
+    if budget_bytes is None:
+        free, _ = torch.cuda.mem_get_info()
+        budget_bytes = int(0.3 * free)
+    nb = nom
+    while nb > 1 and lib.pg_eps_inverse_mixed_workspace(npb, nom, nb) > budget_bytes:
+        nb = (nb + 1) // 2
+    return nb
+
+
+def eps_inverse(eps, npb, nom, epsw1=None, head=None, stream=None, precision=None, work=None, iters=None,
+                omega_batch=None):
+    """ε⁻¹ − 1 in place; for q = 0 also the updated wings and head.
+
+    ``precision='mixed'``: FP32 inverse refined ``iters`` times in FP64 with the
+    residual on the tensor cores (``pg_eps_inverse_mixed``); otherwise the FP64
+    Gauss–Jordan inverse (``pg_eps_inverse_f64``)."""
+    lib = _lib.load()
+    precision = precision or PRECISION
     epsw2 = None
     head_d = None
     if epsw1 is not None:
         epsw2 = torch.conj(epsw1).resolve_conj().contiguous()
         head_d = to_device(np.asarray(head, dtype=np.complex128), torch.complex128).clone()
-    wb = lib.pg_eps_inverse_f64_workspace(npb, nom)
-    if work is None or work.numel() < wb:
-        work = workspace(wb)
-    rc = lib.pg_eps_inverse_f64(ptr(eps), npb, nom, ptr(epsw1), ptr(epsw2), ptr(head_d), ptr(work), work.numel(),
-                                stream_handle(stream))
-    _lib.check(rc, "pg_eps_inverse_f64")
-    return EpsResult(eps, epsw1, epsw2, head_d, npb, nom)
+    status = None
+    if precision == "mixed":
+        nb = omega_batch or eps_inverse_batch(npb, nom)
+        wb = lib.pg_eps_inverse_mixed_workspace(npb, nom, nb)
+        if work is None or work.numel() < wb:
+            work = workspace(wb)
+        status = torch.zeros(1, dtype=torch.int32, device="cuda")
+        rc = lib.pg_eps_inverse_mixed(ptr(eps), npb, nom, ptr(epsw1), ptr(epsw2), ptr(head_d), ptr(work),
+                                      work.numel(), int(nb), int(REFINE_ITERS if iters is None else iters),
+                                      ptr(status), stream_handle(stream))
+        _lib.check(rc, "pg_eps_inverse_mixed")
+    else:
+        wb = lib.pg_eps_inverse_f64_workspace(npb, nom)
+        if work is None or work.numel() < wb:
+            work = workspace(wb)
+        rc = lib.pg_eps_inverse_f64(ptr(eps), npb, nom, ptr(epsw1), ptr(epsw2), ptr(head_d), ptr(work),
+                                    work.numel(), stream_handle(stream))
+        _lib.check(rc, "pg_eps_inverse_f64")
+    r = EpsResult(eps, epsw1, epsw2, head_d, npb, nom)
+    r.status = status
+    return r
 
 
 def chi0_eps(kcw, minm, nkp, npb, nb1, nb2, nom, pm_k=None, head=None, k_chunk=None, stream=None, precision=None,
@@ -264,8 +300,8 @@ def chi0_eps(kcw, minm, nkp, npb, nb1, nb2, nom, pm_k=None, head=None, k_chunk=N
     if precision == "mixed":
         eps, status, _ = chi0_mixed(kcw_d, minm, nkp, npb, nb1, nb2, nom, stream=stream, timers=timers)
         epsw1 = wings_f64(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k, stream=stream) if pm_k is not None else None
-        r = eps_inverse(eps, npb, nom, epsw1=epsw1, head=head, stream=stream)
-        r.status = status
+        r = eps_inverse(eps, npb, nom, epsw1=epsw1, head=head, stream=stream, precision="mixed")
+        r.chi0_status = status
         return r
     eps, epsw1 = chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=pm_k, k_chunk=k_chunk, stream=stream,
                                  precision=precision, timers=timers)
