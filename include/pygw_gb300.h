@@ -101,6 +101,20 @@ size_t pg_chi0_mixed_workspace(int nb1, int nb2, int nkp, int npb, int omega_bat
 int pg_chi0_mixed(const void* minm, int nkp, const double* kcw, int nb1, int nb2, int nom, int npb, double coef,
                   void* eps, void* work, size_t work_bytes, int omega_batch, int kb_split, unsigned* d_status,
                   void* stream, void* const* gemm_events);
+/* The same contraction for the k-points k0 .. k0+nk_chunk-1 only (minm holds
+ * their blocks, [nk_chunk][P][N]; kcw covers all nkp points), so the matrix
+ * elements can be streamed in k-chunks as the reference builds them one k at a
+ * time (pygw.py:3096-3185): eps = (accumulate ? eps : 0) + χ0 of the chunk.
+ * Each chunk is split with its own row exponents; chunk sums add in FP64.
+ * Ragged band windows: with kstart (device, nk_chunk+1 row offsets into minm)
+ * and knb2 (device, nk_chunk) point i contributes the nb1·knb2[i] pairs of its
+ * first knb2[i] unoccupied bands, pair index ie1·knb2[i] + ie2, nK rows in all
+ * (kstart = NULL: every point has the full nb1·nb2 window).
+ * Workspace: pg_chi0_mixed_workspace with nkp = nk_chunk. */
+int pg_chi0_mixed_accumulate(const void* minm, int nk_chunk, int k0, const int* kstart, const int* knb2, long long nK,
+                             const double* kcw, int nb1, int nb2, int nkp, int nom, int npb, double coef, void* eps,
+                             int accumulate, void* work, size_t work_bytes, int omega_batch, int kb_split,
+                             unsigned* d_status, void* stream, void* const* gemm_events);
 /* Workspace layout (byte offsets and sizes) for inspection by tests. */
 int pg_chi0_mixed_layout(int nb1, int nb2, int nkp, int npb, int omega_batch, int kb_split, size_t* offs,
                          long long* dims);

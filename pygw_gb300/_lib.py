@@ -11,6 +11,7 @@ import os
 from .build import LIB
 
 c_int, c_size_t, c_double, c_void_p = ctypes.c_int, ctypes.c_size_t, ctypes.c_double, ctypes.c_void_p
+c_longlong = ctypes.c_longlong
 c_uint_p = ctypes.POINTER(ctypes.c_uint)
 c_ull_p = ctypes.POINTER(ctypes.c_ulonglong)
 
@@ -34,6 +35,9 @@ SIGNATURES = {
     "pg_eps_inverse_mixed_workspace": (c_size_t, [c_int, c_int, c_int]),
     "pg_eps_inverse_mixed": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_int,
                                      c_int, c_void_p, c_void_p]),
+    "pg_chi0_mixed_accumulate": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_longlong, c_void_p, c_int,
+                                         c_int, c_int, c_int, c_int, c_double, c_void_p, c_int, c_void_p, c_size_t,
+                                         c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "pg_chi0_mixed_layout": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
     "pg_wings_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_int, c_int, c_int, c_double,
                              c_void_p, c_void_p, c_void_p]),

@@ -512,17 +512,37 @@ __global__ void k_digits_A(const double2* __restrict__ minm, long long K, int N,
 }
 
 // Weights for a batch of frequencies: c·w as an FP32 pair (hi + lo ≈ 48 bits).
-__global__ void k_weights_prep(const double* __restrict__ kcw, int nb1, int nb2, int nkp, int om0, int wb, double coef,
-                               long long K, long long K_pad, float2* wpair) {
+// K-value k of the chunk → (point kpt, pair pp): uniform windows (kstart null)
+// have P = nb1·nb2 pairs per point; ragged ones have nb1·knb2[kpt] pairs
+// starting at kstart[kpt], pp = ib·knb2[kpt] + jb.
+__global__ void k_weights_prep(const double* __restrict__ kcw, int nb1, int nb2, int nkp, int k0, int nkc,
+                               const int* __restrict__ kstart, const int* __restrict__ knb2, int om0, int wb,
+                               double coef, long long K, long long K_pad, float2* wpair) {
   const int kb = blockIdx.x, wl = blockIdx.y;
   const int P = nb1 * nb2;
   for (int j = threadIdx.x; j < KB; j += blockDim.x) {
     const long long k = (long long)kb * KB + j;
     float2 pr = make_float2(0.0f, 0.0f);
     if (k < K) {
-      const int kpt = (int)(k / P), pp = (int)(k - (long long)kpt * P);
-      const int ib = pp / nb2, jb = pp - ib * nb2;
-      const double w = coef * kcw[(size_t)ib + (size_t)nb1 * ((size_t)jb + (size_t)nb2 * ((size_t)kpt + (size_t)nkp * (om0 + wl)))];
+      int kpt, ib, jb;
+      if (kstart) {
+        int lo = 0, hi = nkc;                    // kstart[lo] ≤ k < kstart[hi]
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if ((long long)kstart[mid] <= k) lo = mid; else hi = mid;
+        }
+        kpt = lo;
+        const int pp = (int)(k - kstart[kpt]), n2 = knb2[kpt];
+        ib = pp / n2;
+        jb = pp - ib * n2;
+      } else {
+        kpt = (int)(k / P);
+        const int pp = (int)(k - (long long)kpt * P);
+        ib = pp / nb2;
+        jb = pp - ib * nb2;
+      }
+      const double w =
+          coef * kcw[(size_t)ib + (size_t)nb1 * ((size_t)jb + (size_t)nb2 * ((size_t)(k0 + kpt) + (size_t)nkp * (om0 + wl)))];
       const float hi = __double2float_rn(w);
       const float lo = __double2float_rn(w - (double)hi);
       pr = make_float2(hi, lo);
@@ -649,7 +669,7 @@ __global__ void k_digits_B(const __nv_bfloat16* __restrict__ adig, const int* eA
 
 // χ0[ω][J][I] (complex, full matrix) from the digit-group sums.
 __global__ void k_assemble(const double* __restrict__ out, const int* eA, const int* fB, int N, int R_pad, int nT,
-                           int npair, int nsplit, int wb, int om0, double2* __restrict__ eps) {
+                           int npair, int nsplit, int wb, int om0, int accumulate, double2* __restrict__ eps) {
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y;
   const int wl = blockIdx.z;
@@ -666,7 +686,9 @@ __global__ void k_assemble(const double* __restrict__ out, const int* eA, const 
   };
   const double re = G(I, J) + G(N + I, N + J);
   const double im = G(N + I, J) - G(I, N + J);
-  eps[((size_t)(om0 + wl) * N + J) * N + I] = make_double2(re, im);
+  double2& e = eps[((size_t)(om0 + wl) * N + J) * N + I];
+  if (accumulate) e = make_double2(e.x + re, e.y + im);
+  else e = make_double2(re, im);
 }
 
 }  // namespace pgm
@@ -717,9 +739,9 @@ static int gemm_cta_capacity() {
   return g_cap[dev];
 }
 
-static MixedLayout mixed_layout(int nb1, int nb2, int nkp, int npb, int wb, int kb_split) {
+static MixedLayout mixed_layout(int nb1, int nb2, int nkp, int npb, int wb, int kb_split, long long K = -1) {
   MixedLayout L;
-  L.K = (long long)nkp * nb1 * nb2;
+  L.K = K >= 0 ? K : (long long)nkp * nb1 * nb2;
   L.K_pad = (L.K + KB - 1) / KB * KB;
   L.nkb = (int)(L.K_pad / KB);
   L.N = npb;
@@ -804,13 +826,16 @@ extern "C" size_t pg_chi0_mixed_workspace(int nb1, int nb2, int nkp, int npb, in
 // eps[ω][J][I].  Frequencies are processed omega_batch at a time; kb_split
 // (> 0) caps the 64-value K-blocks one CTA sums (0 = the largest exact range).
 // gemm_events (optional): 2 per batch, recorded around each digit-GEMM launch.
-extern "C" int pg_chi0_mixed(const void* minm, int nkp, const double* kcw, int nb1, int nb2, int nom, int npb,
-                             double coef, void* eps, void* work, size_t work_bytes, int omega_batch, int kb_split,
-                             unsigned* d_status, void* stream, void* const* gemm_events) {
-  if (!minm || !kcw || !eps || !work || nkp <= 0 || nb1 <= 0 || nb2 <= 0 || nom <= 0 || npb <= 0 || omega_batch <= 0)
+static int chi0_mixed_impl(const void* minm, int nkp, int k0, const int* kstart, const int* knb2, long long nK,
+                           int nkp_total, const double* kcw, int nb1, int nb2, int nom, int npb, double coef, void* eps,
+                           int accumulate, void* work, size_t work_bytes, int omega_batch, int kb_split,
+                           unsigned* d_status, void* stream, void* const* gemm_events) {
+  if (!minm || !kcw || !eps || !work || nkp <= 0 || nb1 <= 0 || nb2 <= 0 || nom <= 0 || npb <= 0 || omega_batch <= 0 ||
+      k0 < 0 || k0 + nkp > nkp_total)
     return PG_EARG;
+  if (kstart && (!knb2 || nK <= 0 || nK > (long long)nkp * nb1 * nb2)) return PG_EARG;
   const int wb = omega_batch < nom ? omega_batch : nom;
-  MixedLayout L = mixed_layout(nb1, nb2, nkp, npb, wb, kb_split);
+  MixedLayout L = mixed_layout(nb1, nb2, nkp, npb, wb, kb_split, kstart ? nK : -1);
   if (work_bytes < L.total) return PG_EWORKSPACE;
   if (L.R_pad > (1 << 20) || L.K_pad > (1ll << 31)) return PG_ETOOBIG;
   cudaStream_t s = (cudaStream_t)stream;
@@ -851,7 +876,8 @@ extern "C" int pg_chi0_mixed(const void* minm, int nkp, const double* kcw, int n
   attr[0].val.clusterDim.z = 1;
   for (int om0 = 0; om0 < nom; om0 += wb) {
     const int nw = (om0 + wb <= nom) ? wb : nom - om0;
-    k_weights_prep<<<dim3(L.nkb, nw), 64, 0, s>>>(kcw, nb1, nb2, nkp, om0, nw, coef, L.K, L.K_pad, wpair);
+    k_weights_prep<<<dim3(L.nkb, nw), 64, 0, s>>>(kcw, nb1, nb2, nkp_total, k0, nkp, kstart, knb2, om0, nw, coef,
+                                                  L.K, L.K_pad, wpair);
     if (cudaMemsetAsync(rmax, 0, (size_t)L.wb * L.R_pad * 4, s) != cudaSuccess) return PG_ECUDA;
     k_rowmax_B<<<dim3((unsigned)((L.K_pad + 1023) / 1024), L.R_pad), 256, 0, s>>>(adig, wpair, L.R, L.R_pad, L.K_pad,
                                                                                   nw, rmax);
@@ -870,10 +896,34 @@ extern "C" int pg_chi0_mixed(const void* minm, int nkp, const double* kcw, int n
     if (cudaLaunchKernelEx(&cfg, k_ozaki_gemm<S>, mapA, mapB, op) != cudaSuccess) return PG_ECUDA;
     if (gemm_events && cudaEventRecord((cudaEvent_t)gemm_events[2 * batch + 1], s) != cudaSuccess) return PG_ECUDA;
     k_assemble<<<dim3((npb + 127) / 128, npb, nw), 128, 0, s>>>(out, eA, fB, npb, L.R_pad, L.nT, L.npair, L.nsplit,
-                                                               wb, om0, (double2*)eps);
+                                                               wb, om0, accumulate, (double2*)eps);
     pg_count_launches(6);
   }
   return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ECUDA;
+}
+
+extern "C" int pg_chi0_mixed(const void* minm, int nkp, const double* kcw, int nb1, int nb2, int nom, int npb,
+                             double coef, void* eps, void* work, size_t work_bytes, int omega_batch, int kb_split,
+                             unsigned* d_status, void* stream, void* const* gemm_events) {
+  return chi0_mixed_impl(minm, nkp, 0, nullptr, nullptr, 0, nkp, kcw, nb1, nb2, nom, npb, coef, eps, 0, work,
+                         work_bytes, omega_batch, kb_split, d_status, stream, gemm_events);
+}
+
+// The same for the k-points k0 .. k0+nk_chunk−1 (minm holds their blocks;
+// kcw covers all nkp points): eps = (accumulate ? eps : 0) + their χ0.  Each
+// chunk has its own row exponents; the chunks' sums add in FP64.  With
+// kstart (device, nk_chunk+1 offsets) and knb2 (device, nk_chunk counts) the
+// points have ragged windows: point i contributes nb1·knb2[i] pairs (the
+// first knb2[i] of the nb2 unoccupied bands), its rows of minm starting at
+// kstart[i], nK = kstart[nk_chunk] in all.  Workspace:
+// pg_chi0_mixed_workspace(nb1, nb2, nk_chunk, npb, omega_batch, kb_split).
+extern "C" int pg_chi0_mixed_accumulate(const void* minm, int nk_chunk, int k0, const int* kstart, const int* knb2,
+                                        long long nK, const double* kcw, int nb1, int nb2, int nkp, int nom, int npb,
+                                        double coef, void* eps, int accumulate, void* work, size_t work_bytes,
+                                        int omega_batch, int kb_split, unsigned* d_status, void* stream,
+                                        void* const* gemm_events) {
+  return chi0_mixed_impl(minm, nk_chunk, k0, kstart, knb2, nK, nkp, kcw, nb1, nb2, nom, npb, coef, eps, accumulate,
+                         work, work_bytes, omega_batch, kb_split, d_status, stream, gemm_events);
 }
 
 // Full product for the refinement of ε⁻¹ (see ozaki.h).

@@ -4,7 +4,8 @@
 // The ε block of calc_eps (pygw.py:3229-3271) inverts the Hermitian
 // A = (ε + εᴴ)/2 + I per frequency with scipy.linalg.inv in FP64.  Here:
 //   1. X0 = A⁻¹ in FP32 (complex Gauss–Jordan, partial pivoting by |Re|+|Im|,
-//      the same algorithm as the FP64 path);
+//      the FP64 path's algorithm, blocked: panels of b columns factored in
+//      shared memory, then a rank-b update of the other columns);
 //   2. `iters` refinement steps  R = I − A·X (split-precision digit GEMM on
 //      tcgen05: A and X split into six 8-bit digits per value, digit pairs
 //      s + t ≤ 5 summed exactly, ≈ 2^-48 relative to the row scales),
@@ -52,74 +53,131 @@ __global__ void k_to_f32(const double2* __restrict__ a, float2* __restrict__ x, 
   if (i < n) x[i] = make_float2((float)a[i].x, (float)a[i].y);
 }
 
-// Pivot search, row swap and pivot-row scaling for step k (one block per ω).
-__global__ void k_gj32_pivot(float2* X, int N, int k, int* perm) {
+// ---- blocked Gauss–Jordan: the same elimination (partial pivoting by
+// |Re|+|Im|, first on ties; row swaps over the whole matrix; the inverse
+// built in place) organised in panels of b columns.  Within a panel the b
+// elementary steps are applied to the panel columns only; their product M
+// differs from I only in the panel's (pivot) rows, so the other columns follow
+// as A_o ← A_o + W·S − I_p·S with W the factored panel columns and S the
+// panel rows of A_o (a rank-b update).
+
+// Panel factorisation, one CTA per ω; the panel (N × b) lives in shared memory
+// as P[j][i].  Row swaps of the non-panel columns are made here in global
+// memory (they precede the rank-b update of those columns).
+__global__ void __launch_bounds__(512) k_gj32_panel(float2* X, int N, int c0, int b, int* perm) {
+  extern __shared__ float2 Pn[];                 // [b][N]
+  __shared__ float sv[512];
+  __shared__ int si[512];
   const int w = blockIdx.x;
   float2* E = X + (size_t)N * N * w;
-  __shared__ float sv[256];
-  __shared__ int si[256];
-  float best = -1.0f;
-  int bi = N;
-  for (int i = k + threadIdx.x; i < N; i += blockDim.x) {
-    const float2 a = E[(size_t)i + (size_t)N * k];
-    const float v = fabsf(a.x) + fabsf(a.y);
-    if (v > best) { best = v; bi = i; }
+  for (int e = threadIdx.x; e < b * N; e += blockDim.x) {
+    const int j = e / N, i = e - j * N;
+    Pn[e] = E[(size_t)i + (size_t)N * (c0 + j)];
   }
-  sv[threadIdx.x] = best;
-  si[threadIdx.x] = bi;
   __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      const float v2 = sv[threadIdx.x + s];
-      const int i2 = si[threadIdx.x + s];
-      if (v2 > sv[threadIdx.x] || (v2 == sv[threadIdx.x] && i2 < si[threadIdx.x])) {
-        sv[threadIdx.x] = v2;
-        si[threadIdx.x] = i2;
+  for (int jj = 0; jj < b; jj++) {
+    const int k = c0 + jj;
+    float2* col = Pn + (size_t)jj * N;
+    float best = -1.0f;
+    int bi = N;
+    for (int i = k + threadIdx.x; i < N; i += blockDim.x) {
+      const float v = fabsf(col[i].x) + fabsf(col[i].y);
+      if (v > best) { best = v; bi = i; }
+    }
+    sv[threadIdx.x] = best;
+    si[threadIdx.x] = bi;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        const float v2 = sv[threadIdx.x + s];
+        const int i2 = si[threadIdx.x + s];
+        if (v2 > sv[threadIdx.x] || (v2 == sv[threadIdx.x] && i2 < si[threadIdx.x])) {
+          sv[threadIdx.x] = v2;
+          si[threadIdx.x] = i2;
+        }
+      }
+      __syncthreads();
+    }
+    const int p = (si[0] < N) ? si[0] : k;       // a column without a finite pivot keeps its row
+    if (threadIdx.x == 0) perm[(size_t)N * w + k] = p;
+    if (p != k) {
+      for (int c = threadIdx.x; c < N; c += blockDim.x) {
+        if (c >= c0 && c < c0 + b) {
+          float2* pc = Pn + (size_t)(c - c0) * N;
+          const float2 t = pc[k]; pc[k] = pc[p]; pc[p] = t;
+        } else {
+          const float2 t = E[(size_t)k + (size_t)N * c];
+          E[(size_t)k + (size_t)N * c] = E[(size_t)p + (size_t)N * c];
+          E[(size_t)p + (size_t)N * c] = t;
+        }
       }
     }
     __syncthreads();
+    const float2 r = crecipf(col[k]);
+    __syncthreads();
+    // pivot row of the panel: scaled; the pivot itself becomes 1/pivot
+    for (int j = threadIdx.x; j < b; j += blockDim.x) {
+      if (j == jj) Pn[(size_t)j * N + k] = r;
+      else Pn[(size_t)j * N + k] = cmulf(Pn[(size_t)j * N + k], r);
+    }
+    __syncthreads();
+    // other rows: P[j][i] −= P[jj][i]·P[j][k] (j ≠ jj), then P[jj][i] = −P[jj][i]·r
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      if (i == k) continue;
+      const float2 f = col[i];
+      for (int j = 0; j < b; j++) {
+        if (j == jj) continue;
+        float2& d = Pn[(size_t)j * N + i];
+        const float2 a = Pn[(size_t)j * N + k];
+        d.x -= f.x * a.x - f.y * a.y;
+        d.y -= f.x * a.y + f.y * a.x;
+      }
+      const float2 v = cmulf(f, r);
+      col[i] = make_float2(-v.x, -v.y);
+    }
+    __syncthreads();
   }
-  const int p = (si[0] < N) ? si[0] : k;   // a column without a finite pivot keeps its row
-  if (threadIdx.x == 0) perm[(size_t)N * w + k] = p;
-  if (p != k) {
-    for (int j = threadIdx.x; j < N; j += blockDim.x) {
-      const float2 t = E[(size_t)k + (size_t)N * j];
-      E[(size_t)k + (size_t)N * j] = E[(size_t)p + (size_t)N * j];
-      E[(size_t)p + (size_t)N * j] = t;
+  for (int e = threadIdx.x; e < b * N; e += blockDim.x) {
+    const int j = e / N, i = e - j * N;
+    E[(size_t)i + (size_t)N * (c0 + j)] = Pn[e];
+  }
+}
+
+// Rank-b update of the non-panel columns: A[i,c] ← (i in panel ? 0 : A[i,c]) + Σ_j W[i,j]·S[j,c],
+// S[j,c] = A[c0+j, c] read before any write of column c.  Block: 32 columns
+// (panel columns skipped) × all rows of one ω; grid (ceil(N/32), nw).
+constexpr int GJ_BMAX = 16;
+__global__ void __launch_bounds__(256) k_gj32_update(float2* X, int N, int c0, int b) {
+  __shared__ float2 Ss[GJ_BMAX][32];
+  const int w = blockIdx.y;
+  const int cbase = blockIdx.x * 32;
+  float2* E = X + (size_t)N * N * w;
+  for (int e = threadIdx.x; e < b * 32; e += blockDim.x) {
+    const int j = e / 32, cc = e % 32, c = cbase + cc;
+    Ss[j][cc] = (c < N && (c < c0 || c >= c0 + b)) ? E[(size_t)(c0 + j) + (size_t)N * c] : make_float2(0.0f, 0.0f);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    float2 wr[GJ_BMAX];
+#pragma unroll
+    for (int j = 0; j < GJ_BMAX; j++) wr[j] = (j < b) ? E[(size_t)i + (size_t)N * (c0 + j)] : make_float2(0.0f, 0.0f);
+    const bool prow = i >= c0 && i < c0 + b;
+    for (int cc = 0; cc < 32; cc++) {
+      const int c = cbase + cc;
+      if (c >= N) break;
+      if (c >= c0 && c < c0 + b) continue;
+      float2 acc = prow ? make_float2(0.0f, 0.0f) : E[(size_t)i + (size_t)N * c];
+#pragma unroll
+      for (int j = 0; j < GJ_BMAX; j++) {
+        if (j < b) {
+          const float2 sj = Ss[j][cc];
+          acc.x += wr[j].x * sj.x - wr[j].y * sj.y;
+          acc.y += wr[j].x * sj.y + wr[j].y * sj.x;
+        }
+      }
+      E[(size_t)i + (size_t)N * c] = acc;
     }
   }
-  __syncthreads();
-  const float2 r = crecipf(E[(size_t)k + (size_t)N * k]);
-  __syncthreads();
-  for (int j = threadIdx.x; j < N; j += blockDim.x) {
-    if (j == k) E[(size_t)k + (size_t)N * k] = r;
-    else E[(size_t)k + (size_t)N * j] = cmulf(E[(size_t)k + (size_t)N * j], r);
-  }
-}
-
-// X[i,j] −= X[i,k]·X[k,j] for i ≠ k, j ≠ k.
-__global__ void k_gj32_eliminate(float2* X, int N, int k) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
-  const int w = blockIdx.z;
-  if (i >= N || i == k || j == k) return;
-  float2* E = X + (size_t)N * N * w;
-  const float2 f = E[(size_t)i + (size_t)N * k];
-  const float2 a = E[(size_t)k + (size_t)N * j];
-  float2& d = E[(size_t)i + (size_t)N * j];
-  d.x -= f.x * a.x - f.y * a.y;
-  d.y -= f.x * a.y + f.y * a.x;
-}
-
-// X[i,k] ← −X[i,k]·X[k,k] for i ≠ k (X[k,k] already holds 1/pivot).
-__global__ void k_gj32_column(float2* X, int N, int k) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int w = blockIdx.y;
-  if (i >= N || i == k) return;
-  float2* E = X + (size_t)N * N * w;
-  const float2 r = E[(size_t)k + (size_t)N * k];
-  const float2 v = cmulf(E[(size_t)i + (size_t)N * k], r);
-  E[(size_t)i + (size_t)N * k] = make_float2(-v.x, -v.y);
 }
 
 // Undo the row interchanges on the columns of the inverse (reverse order).
@@ -391,21 +449,28 @@ extern "C" int pg_eps_inverse_mixed(void* eps_, int npb, int nom, void* epsw1_, 
   double2* x64 = (double2*)(w + L.x64);
   int* eA = (int*)(w + L.eA);
   __nv_bfloat16* adig = (__nv_bfloat16*)(w + L.adig);
-  const int TB = 128;
   pge::launch_sym_add_identity(eps, N, nom, s);
   for (int w0 = 0; w0 < nom; w0 += nb) {
     const int nw = (w0 + nb <= nom) ? nb : nom - w0;
     double2* A = eps + NN * w0;
     const size_t n = NN * nw;
     k_to_f32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A, x32, n);
-    dim3 gsq((N + TB - 1) / TB, N, nw);
-    for (int k = 0; k < N; k++) {
-      k_gj32_pivot<<<nw, 256, 0, s>>>(x32, N, k, perm);
-      k_gj32_eliminate<<<gsq, TB, 0, s>>>(x32, N, k);
-      k_gj32_column<<<dim3((N + TB - 1) / TB, nw), TB, 0, s>>>(x32, N, k);
+    // panel width: the panel (b × N complex floats) must fit in shared memory
+    int bw = GJ_BMAX;
+    while (bw > 1 && (size_t)bw * N * sizeof(float2) > (size_t)200 * 1024) bw /= 2;
+    const size_t psm = (size_t)bw * N * sizeof(float2);
+    if (psm > (size_t)200 * 1024) return PG_ETOOBIG;
+    if (cudaFuncSetAttribute(k_gj32_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm) != cudaSuccess)
+      return PG_ECUDA;
+    unsigned long long nl = 2;
+    for (int c0 = 0; c0 < N; c0 += bw) {
+      const int b = (c0 + bw <= N) ? bw : N - c0;
+      k_gj32_panel<<<nw, 512, psm, s>>>(x32, N, c0, b, perm);
+      k_gj32_update<<<dim3((N + 31) / 32, nw), 256, 0, s>>>(x32, N, c0, b);
+      nl += 2;
     }
     k_gj32_unpermute<<<nw, 256, 0, s>>>(x32, N, perm);
-    pg_count_launches(2 + 3ull * N);
+    pg_count_launches(nl);
     if (iters == 0) {
       k_to_f64<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x32, A, n);
       pg_count_launches(1);

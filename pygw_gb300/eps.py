@@ -52,7 +52,8 @@ def _kcw_device(kcw):
     return to_device(a.transpose(3, 2, 1, 0), torch.float64)
 
 
-def _launch_chi0(lib, mk, kc, k0, kcw_d, nb1, nb2, nkp, nom, npb, eps, pmd, epsw1, stream, timers, precision):
+def _launch_chi0(lib, mk, kc, k0, kcw_d, nb1, nb2, nkp, nom, npb, eps, pmd, epsw1, stream, timers, precision,
+                 mctx=None):
     sh = stream_handle(stream)
     ev = None
     if timers is not None:
@@ -63,6 +64,17 @@ def _launch_chi0(lib, mk, kc, k0, kcw_d, nb1, nb2, nkp, nom, npb, eps, pmd, epsw
         rc = lib.pg_chi0_accumulate_f64(ptr(mk), kc, k0, ptr(kcw_d), nb1, nb2, nkp, nom, npb, -FSPIN, ptr(eps),
                                         ptr(pmd), ptr(epsw1) if pmd is not None else None, sh)
         _lib.check(rc, "pg_chi0_accumulate_f64")
+    elif precision == "mixed":
+        # split-precision χ0 of this k-chunk added to eps; q = 0 wings in FP64
+        rc = lib.pg_chi0_mixed_accumulate(ptr(mk), kc, k0, None, None, 0, ptr(kcw_d), nb1, nb2, nkp, nom, npb,
+                                          -FSPIN, ptr(eps), 1 if mctx["started"] else 0, ptr(mctx["work"]),
+                                          mctx["work"].numel(), int(mctx["wb"]), 0, ptr(mctx["status"]), sh, None)
+        _lib.check(rc, "pg_chi0_mixed_accumulate")
+        mctx["started"] = True
+        if pmd is not None:
+            rc = lib.pg_wings_f64(ptr(mk), kc, k0, ptr(kcw_d), nb1, nb2, nkp, nom, npb, -FSPIN, ptr(pmd), ptr(epsw1),
+                                  sh)
+            _lib.check(rc, "pg_wings_f64")
     else:
         raise ValueError(f"unknown precision {precision!r}")
     if ev is not None:
@@ -71,7 +83,7 @@ def _launch_chi0(lib, mk, kc, k0, kcw_d, nb1, nb2, nkp, nom, npb, eps, pmd, epsw
 
 
 def chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=None, k_chunk=None, stream=None, eps=None,
-                    epsw1=None, precision=None, timers=None):
+                    epsw1=None, precision=None, timers=None, status=None):
     """Σ_k of the weighted rank-P updates into ``eps`` (and ``epsw1`` for q = 0).
 
     ``minm`` is either a callable ``minm(ik) -> minm[nb1, nb2, npb]`` (numpy or
@@ -79,6 +91,8 @@ def chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=None, k_chunk=Non
     ``[nkp, P, npb]`` — on the device (used in place) or in pinned host memory
     (streamed in k-chunks on a side stream, double-buffered against the
     contraction).  ``pm_k(ik)`` returns the q→0 vector ``pm[P]``.
+    ``precision='mixed'`` runs the split-precision tensor-core contraction per
+    k-chunk (``status``, a device int32 tensor, receives its PG_ERR_* bits).
     ``timers`` (a list) receives a CUDA event pair around each χ0 launch.
     """
     precision = precision or PRECISION
@@ -89,8 +103,20 @@ def chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=None, k_chunk=Non
         eps = torch.zeros((nom, npb, npb), dtype=torch.complex128, device="cuda")
     if pm_k is not None and epsw1 is None:
         epsw1 = torch.zeros((nom, npb), dtype=torch.complex128, device="cuda")
-    if k_chunk is None:
-        k_chunk = max(1, min(nkp, (256 << 20) // max(1, P * npb * 16)))
+    on_device = isinstance(minm, torch.Tensor) and minm.is_cuda
+    if on_device:
+        k_chunk = nkp                    # resident: one pass over all k
+    elif k_chunk is None:
+        # the tensor-core contraction wants long K per launch: bigger chunks
+        budget = (4 << 30) if precision == "mixed" else (256 << 20)
+        k_chunk = max(1, min(nkp, budget // max(1, P * npb * 16)))
+    mctx = None
+    if precision == "mixed":
+        kc_max = min(k_chunk, nkp)
+        wb = mixed_omega_batch(nb1, nb2, kc_max, npb, nom)
+        mctx = {"wb": wb, "started": False,
+                "work": workspace(lib.pg_chi0_mixed_workspace(nb1, nb2, kc_max, npb, wb, 0)),
+                "status": status if status is not None else torch.zeros(1, dtype=torch.int32, device="cuda")}
 
     def pm_chunk(k0, kc):
         if pm_k is None:
@@ -98,12 +124,10 @@ def chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=None, k_chunk=Non
         return to_device(np.stack([np.asarray(pm_k(ik), dtype=np.complex128) for ik in range(k0, k0 + kc)]),
                          torch.complex128)
 
-    if isinstance(minm, torch.Tensor) and minm.is_cuda:
+    if on_device:
         m = minm.reshape(nkp, P, npb)
-        for k0 in range(0, nkp, nkp if pm_k is None else k_chunk):
-            kc = min(nkp if pm_k is None else k_chunk, nkp - k0)
-            _launch_chi0(lib, m[k0:k0 + kc], kc, k0, kcw_d, nb1, nb2, nkp, nom, npb, eps, pm_chunk(k0, kc), epsw1,
-                         stream, timers, precision)
+        _launch_chi0(lib, m, nkp, 0, kcw_d, nb1, nb2, nkp, nom, npb, eps, pm_chunk(0, nkp), epsw1, stream, timers,
+                     precision, mctx)
         return eps, epsw1
 
     if isinstance(minm, torch.Tensor):
@@ -130,7 +154,7 @@ def chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=None, k_chunk=Non
                 copied[b].record(copy_stream)
             cur.wait_event(copied[b])
             _launch_chi0(lib, bufs[b], kc, k0, kcw_d, nb1, nb2, nkp, nom, npb, eps, pm_chunk(k0, kc), epsw1, stream,
-                         timers, precision)
+                         timers, precision, mctx)
             used[b] = torch.cuda.Event()
             used[b].record(cur)
         return eps, epsw1
@@ -147,7 +171,7 @@ def chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=None, k_chunk=Non
         mk = torch.stack(blocks)
         mk = mk if mk.is_cuda else mk.cuda()
         _launch_chi0(lib, mk, kc, k0, kcw_d, nb1, nb2, nkp, nom, npb, eps, pm_chunk(k0, kc), epsw1, stream, timers,
-                     precision)
+                     precision, mctx)
     return eps, epsw1
 
 
@@ -298,8 +322,9 @@ def chi0_eps(kcw, minm, nkp, npb, nb1, nb2, nom, pm_k=None, head=None, k_chunk=N
     kcw_d = _kcw_device(kcw)
     precision = precision or PRECISION
     if precision == "mixed":
-        eps, status, _ = chi0_mixed(kcw_d, minm, nkp, npb, nb1, nb2, nom, stream=stream, timers=timers)
-        epsw1 = wings_f64(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k, stream=stream) if pm_k is not None else None
+        status = torch.zeros(1, dtype=torch.int32, device="cuda")
+        eps, epsw1 = chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=pm_k, k_chunk=k_chunk, stream=stream,
+                                     precision="mixed", timers=timers, status=status)
         r = eps_inverse(eps, npb, nom, epsw1=epsw1, head=head, stream=stream, precision="mixed")
         r.chi0_status = status
         return r

@@ -121,11 +121,13 @@ def test_mixed_chi0_and_inverse_accuracy(name, kw):
     torch.cuda.synchronize()
     assert int(status.item()) == 0
     chi0 = eps.cpu().numpy().transpose(2, 1, 0)
-    assert _row_scaled_err(chi0, chi0_ref) < 1e-10
+    e_chi0 = _row_scaled_err(chi0, chi0_ref)
+    assert e_chi0 < 1e-10
     r = peps.chi0_eps(kcw, lambda ik: minm[ik], nkp, w.npb, nb1, nb2, nom, precision="mixed")
     einv = r.numpy()[0] + np.eye(w.npb)[:, :, None]
     einv_ref = ref[0] + np.eye(w.npb)[:, :, None]
     rel = max(np.max(np.abs(einv[..., o] - einv_ref[..., o])) / np.max(np.abs(einv_ref[..., o])) for o in range(nom))
+    print(f"{name}: chi0 row-scaled {e_chi0:.2e}, eps^-1 max rel {rel:.2e}")
     assert rel < 1e-9, rel
 
 
@@ -141,3 +143,29 @@ def test_mixed_q0_wings_and_head():
     eps, w1, w2, head = r.numpy()
     assert np.max(np.abs(head - ref[3])) / np.max(np.abs(ref[3])) < 1e-9
     assert np.max(np.abs(w1 - ref[1])) / np.max(np.abs(ref[1])) < 1e-9
+
+
+def test_mixed_streamed_chunks_match_resident():
+    """k-chunked split-precision χ0 (callable and pinned-host inputs, several
+    chunks, q→0 wings) against the one-pass contraction over resident k."""
+    w = syn.scaled(syn.WORKLOADS["C1"], div=3, npb=96, nom=4)
+    p, kcw, minm = _problem(w)
+    nb1, nb2, nkp, nom = kcw.shape
+    P, N = nb1 * nb2, w.npb
+    pms = [syn.pm_k(w, p.bands, ik) for ik in range(nkp)]
+    kd = peps._kcw_device(kcw)
+    eps_all, status, _ = peps.chi0_mixed(kd, lambda ik: minm[ik], nkp, N, nb1, nb2, nom)
+    w1_all = peps.wings_f64(kd, lambda ik: minm[ik], nkp, N, nb1, nb2, nom, lambda ik: pms[ik])
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    ref = eps_all.cpu().numpy().transpose(2, 1, 0)
+    host = torch.from_numpy(np.stack([m.reshape(P, N) for m in minm])).pin_memory()
+    for src, kc in ((lambda ik: minm[ik], 3), (host, 4)):
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        eps, w1 = peps.chi0_accumulate(kd, src, nkp, N, nb1, nb2, nom, pm_k=lambda ik: pms[ik], k_chunk=kc,
+                                       precision="mixed", status=st)
+        torch.cuda.synchronize()
+        assert int(st.item()) == 0
+        got = eps.cpu().numpy().transpose(2, 1, 0)
+        assert _row_scaled_err(got, ref) < 1e-10      # each is within ~3e-11 of the FP64 oracle
+        assert np.max(np.abs(w1.cpu().numpy() - w1_all.cpu().numpy())) <= 1e-12 * np.max(np.abs(w1_all.cpu().numpy()))
