@@ -140,6 +140,19 @@ size_t pg_eps_inverse_mixed_workspace(int npb, int nom, int omega_batch);
 int pg_eps_inverse_mixed(void* eps, int npb, int nom, void* epsw1, void* epsw2, void* head, void* work,
                          size_t work_bytes, int omega_batch, int iters, unsigned* d_status, void* stream);
 
+/* ------------------------------------------------ synthetic inputs
+ * Matrix elements of the measured synthetic workloads, drawn on the device
+ * for the k-points k0 .. k0+nk-1 of one q: out[rows][N] complex128,
+ *   M = z·√(1/2)/(1 + |E_n(k) − E_m(k−q)|)·√v_I,  z ~ CN(0,1) keyed by (seed, q, k, n, m, I),
+ * rows = nk·nb1·nb2, or nrows with ragged windows (kstart/knb2 as in
+ * pg_chi0_mixed_accumulate).  enk [nbnd][nkp] (weights layout), kqid (nkp,
+ * this q's k−q indices), sqv (N) √v_I.  No counterpart in the reference
+ * (its matrix elements come from the LAPW code); used by the large
+ * benchmarks, which stream M per k-chunk without holding it all. */
+int pg_synth_minm(int nk, int k0, int iq, const double* enk, int nbnd, const int* kqid, int ncg, int numin, int nb1,
+                  int nb2, const int* kstart, const int* knb2, long long nrows, const double* sqv, int npb,
+                  unsigned long long seed, void* out, void* stream);
+
 /* ------------------------------------------------------------ bookkeeping
  * Number of kernels this library has enqueued since it was loaded (all entry
  * points, all streams).  No counterpart in the reference. */

@@ -38,6 +38,8 @@ SIGNATURES = {
     "pg_chi0_mixed_accumulate": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_longlong, c_void_p, c_int,
                                          c_int, c_int, c_int, c_int, c_double, c_void_p, c_int, c_void_p, c_size_t,
                                          c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    "pg_synth_minm": (c_int, [c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_int, c_void_p,
+                              c_void_p, c_longlong, c_void_p, c_int, ctypes.c_ulonglong, c_void_p, c_void_p]),
     "pg_chi0_mixed_layout": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
     "pg_wings_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_int, c_int, c_int, c_double,
                              c_void_p, c_void_p, c_void_p]),

@@ -27,6 +27,7 @@ SOURCES = {
     "launches.cu": [],
     "chi0_mixed.cu": [],
     "eps_mixed.cu": [],
+    "synth.cu": [],
 }
 
 

@@ -169,3 +169,42 @@ def test_mixed_streamed_chunks_match_resident():
         got = eps.cpu().numpy().transpose(2, 1, 0)
         assert _row_scaled_err(got, ref) < 1e-10      # each is within ~3e-11 of the FP64 oracle
         assert np.max(np.abs(w1.cpu().numpy() - w1_all.cpu().numpy())) <= 1e-12 * np.max(np.abs(w1_all.cpu().numpy()))
+
+
+def test_mixed_ragged_windows_match_zero_padded():
+    """Per-k unoccupied-band windows (ragged K = Σ_k nb1·knb2[k]) through the
+    C-ABI against the uniform window with the excluded pairs' matrix elements
+    set to zero (the same sum), and against the FP64 oracle."""
+    w = syn.scaled(syn.WORKLOADS["C1"], div=3, npb=96, nom=3)
+    p, kcw, minm = _problem(w)
+    nb1, nb2, nkp, nom = kcw.shape
+    N = w.npb
+    rng = np.random.default_rng(12)
+    knb2 = rng.integers(nb2 // 2, nb2 + 1, size=nkp).astype(np.int32)
+    padded = []
+    for ik in range(nkp):
+        m = minm[ik].copy()
+        m[:, knb2[ik]:, :] = 0.0
+        padded.append(m)
+    rag = np.concatenate([minm[ik][:, :knb2[ik], :].reshape(-1, N) for ik in range(nkp)])
+    kstart = np.concatenate([[0], np.cumsum(nb1 * knb2)]).astype(np.int32)
+    lib = _lib.load()
+    kd = peps._kcw_device(kcw)
+    wb = nom
+    work = torch.empty(lib.pg_chi0_mixed_workspace(nb1, nb2, nkp, N, wb, 0), dtype=torch.uint8, device="cuda")
+    eps = torch.empty((nom, N, N), dtype=torch.complex128, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    m_d, ks_d, kn_d = torch.from_numpy(rag).cuda(), torch.from_numpy(kstart).cuda(), torch.from_numpy(knb2).cuda()
+    rc = lib.pg_chi0_mixed_accumulate(m_d.data_ptr(), nkp, 0, ks_d.data_ptr(), kn_d.data_ptr(), int(kstart[-1]),
+                                      kd.data_ptr(), nb1, nb2, nkp, nom, N, -2.0, eps.data_ptr(), 0, work.data_ptr(),
+                                      work.numel(), wb, 0, st.data_ptr(), None, None)
+    assert rc == 0
+    eps_u, st_u, _ = peps.chi0_mixed(kd, lambda ik: padded[ik], nkp, N, nb1, nb2, nom)
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0 and int(st_u.item()) == 0
+    got = eps.cpu().numpy().transpose(2, 1, 0)
+    uni = eps_u.cpu().numpy().transpose(2, 1, 0)
+    ref = oe.calc_eps(kcw, lambda ik: padded[ik], N)[4]
+    ref = (ref + np.conj(ref.transpose(1, 0, 2))) / 2
+    assert _row_scaled_err(got, ref) < 1e-10
+    assert _row_scaled_err(got, uni) < 1e-10
