@@ -344,6 +344,124 @@ def run_reference(a, w, rank):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------- batched workload
+def run_batch_workload(a, w, rank, world, sampler):
+    """C4: the q points of uneven N_PB (and ragged per-k windows) as one
+    captured CUDA graph per step; value = step time / q points of the step."""
+    import torch
+    from pygw_gb300 import _lib
+    from pygw_gb300 import batch as pb
+    from pygw_gb300 import eps as peps
+    from pygw_gb300 import synthetic as syn
+    from pygw_gb300.device import ptr, stream_handle
+    lib = _lib.load()
+    prob = syn.Problem(w)
+    tasks = pb.c4_tasks(prob)[rank::world]
+    t0 = time.time()
+    tuner = pb.Tuner(path=os.path.join(ROOT, "gpurun_out", "tune_c4.json") if os.path.isdir(
+        os.path.join(ROOT, "gpurun_out")) else None)
+    bt = pb.batch_for(prob, tasks, tuner=tuner)
+    bt.capture()
+    setup_s = time.time() - t0
+    stream = torch.cuda.current_stream()
+    for _ in range(a.warmup):
+        bt.run(graph=True)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    wall0 = time.time()
+    ev0.record(stream)
+    for _ in range(a.steps):
+        bt.run(graph=True)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    wall1 = time.time()
+    dt = ev0.elapsed_time(ev1) * 1e-3
+    status = bt.status()
+    nq = len(tasks)
+    value = dt / (a.steps * nq)
+    nb1, nb2, nkp, nom = bt.nb1, bt.nb2, bt.nkp, bt.nom
+    alg = sum(8.0 * t.npb * t.npb * k * nom for t, k in zip(tasks, bt.ktot))   # ragged K = Σ_k nb1·knb2[k]
+    peaks = json.load(open(PEAKS_FILE)) if os.path.exists(PEAKS_FILE) else {}
+    peak = peaks.get("bf16_tflops", 1900.0)
+    roof = {"kernel": "whole step (weights + split-precision chi0 + mixed eps^-1, one graph)", "bound": "tensor",
+            "achieved": alg / (dt / a.steps) / 1e12, "peak": peak, "unit": "TFLOP/s",
+            "frac": alg / (dt / a.steps) / 1e12 / peak, "traffic": None,
+            "note": "algorithmic 8*N_q^2*K_q*Nw summed over q (K_q = ragged window total) / step time; "
+                    "the per-kernel roofline of k_ozaki_gemm is in the C3 line"}
+    # plain FP64 GPU path, one q at a time on the full window: weights and inverse timed in full,
+    # the FP64 contraction on a few k-points (device-generated M) and scaled
+    fp64 = None
+    if a.fp64_k_sample > 0:
+        tot, parts = 0.0, []
+        sample = tasks[:: max(1, len(tasks) // 3)][:3]
+        for t in sample:
+            i = tasks.index(t)
+            nk = min(a.fp64_k_sample, nkp)
+            m = torch.empty((nk * nb1 * nb2, t.npb), dtype=torch.complex128, device="cuda")
+            _lib.check(lib.pg_synth_minm(nk, 0, t.iq, ptr(bt.enk_d), bt.nbnd, ptr(bt.kqid_d[t.iq]), bt.ncg, bt.numin,
+                                         nb1, nb2, None, None, 0, ptr(bt.sqv_d[i]), t.npb, bt.seed, ptr(m),
+                                         stream_handle(None)), "pg_synth_minm")
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            ev[0].record()
+            bt._weights(i, stream_handle(None))
+            ev[1].record()
+            eps = torch.zeros((nom, t.npb, t.npb), dtype=torch.complex128, device="cuda")
+            _lib.check(lib.pg_chi0_accumulate_f64(ptr(m), nk, 0, ptr(bt.kcw), nb1, nb2, nkp, nom, t.npb, -2.0,
+                                                  ptr(eps), None, None, stream_handle(None)), "pg_chi0_accumulate_f64")
+            peps.chi0_finalize(eps, t.npb, nom)
+            ev[2].record()
+            peps.eps_inverse(eps, t.npb, nom, precision="fp64")
+            ev[3].record()
+            torch.cuda.synchronize()
+            sq = (ev[0].elapsed_time(ev[1]) + ev[1].elapsed_time(ev[2]) * nkp / nk + ev[2].elapsed_time(ev[3])) * 1e-3
+            parts.append({"npb": t.npb, "s": sq})
+            tot += sq
+            del m, eps
+        fp64 = {"value": tot / len(sample), "unit": "s/q-point", "per_q": parts,
+                "sample": f"{len(sample)} of {nq} q; FP64 contraction on {min(a.fp64_k_sample, nkp)}/{nkp} "
+                          f"k-points of the full window, scaled"}
+    # end to end: host inputs of the batch to the device, the graph, every q's eps^-1 back to pinned host memory
+    e2e = None
+    if not a.no_e2e:
+        outs = [torch.empty(r.shape, dtype=r.dtype).pin_memory() for r in bt.results]
+        b = prob.bands
+        nomx, numin = b.nomax_numin
+        host_in = [torch.from_numpy(np.ascontiguousarray(b.enk().T)).pin_memory(),
+                   torch.from_numpy(np.ascontiguousarray(prob.kqm.tetc.T.astype(np.int32))).pin_memory(),
+                   torch.from_numpy(prob.fr.omega.copy()).pin_memory()]
+        torch.cuda.synchronize()
+        te0 = time.perf_counter()
+        for _ in range(a.steps):
+            bt.enk_d.copy_(host_in[0], non_blocking=True)
+            bt.tetc_d.copy_(host_in[1], non_blocking=True)
+            bt.om_d.copy_(host_in[2], non_blocking=True)
+            bt.run(graph=True)
+            for o, r in zip(outs, bt.results):
+                o.copy_(r, non_blocking=True)
+        torch.cuda.synchronize()
+        et = time.perf_counter() - te0
+        e2e = {"value": et / (a.steps * nq), "unit": "s/q-point",
+               "h2d_bytes_per_step": int(sum(x.numel() * x.element_size() for x in host_in)),
+               "d2h_bytes_per_step": int(sum(o.numel() * 16 for o in outs))}
+    sampler.stop()
+    clocks = sampler.window(wall0, wall1)
+    sampler.cleanup()
+    if rank == 0:
+        line = {"metric": "s/q-point for chi0+eps^-1 (weights -> chi0 -> eps^-1)", "value": value,
+                "unit": "s/q-point", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+                "ms_per_step": dt / a.steps * 1e3, "higher_is_better": False, "scaling": "weak",
+                "vs_baseline": None, "dtype": "bf16-digits/f32-exact/f64", "data": "synthetic",
+                "config": {"workload": workload_desc(w) + f", N_PB per q {[t.npb for t in tasks]}, per-k "
+                                                          f"unoccupied cutoff 100-300 bands",
+                           "precision": "mixed", "parallelism": "replicas",
+                           "batch": {"q_per_step": nq, "graph": True, "setup_s": setup_s,
+                                     "tuned": [[c.k_chunk, c.omega_batch] for c in bt.choice]},
+                           "l2": "inputs larger than L2 (matrix elements drawn per k-chunk on the device)"},
+                "roofline": roof, "kernel_status": status, "fp64_gpu": fp64, "cpu_baseline": None,
+                "e2e": e2e, "gpu_launches": int(bt.graph_launches * a.steps), "clocks": clocks}
+        print(json.dumps(line), flush=True)
+
+
 # -------------------------------------------------------------------- main
 def main():
     a = parse()
@@ -371,6 +489,8 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from pygw_gb300 import _lib
 
+    if w.npb_range:
+        return run_batch_workload(a, w, rank, world, sampler)
     lib = _lib.load()
     inp = Inputs(w, rank)
     inp.statuses = []
