@@ -50,6 +50,18 @@ int pg_bz_calcqdepw_par2(const double* enk, int nbnd, int nkp, double ef, const 
                          size_t work_bytes, int nom_chunk, unsigned* d_status, unsigned long long* d_counters,
                          void* stream);
 
+/* SVD frequency basis (iopfreq = 5): replaces
+ *     kcw = ft.bz_calcqdepw_par3(enk, ef, kqid, ncg, nomx, numin, dUl, omega, tetc)
+ * (pygw.py:3441; for_tetrahedra.f90:466-542).  The corner weights of every
+ * (tetrahedron, band pair) are projected on dUl (device, (nom, nl) Fortran
+ * order, nom·nl ≤ 6144) before they are accumulated; kcw is
+ * (nb1, nb2, nkp, nl).  All frequencies are evaluated in one pass. */
+size_t pg_bz_calcqdepw_par3_workspace(int nbnd, int nkp, int ncg, int nomx, int numin, int nom, int ntet, int nl);
+int pg_bz_calcqdepw_par3(const double* enk, int nbnd, int nkp, double ef, const int* kqid, int ncg, int nomx,
+                         int numin, const double* dUl, int nl, const double* omega, int nom, const int* tetc, int ntet,
+                         double* kcw, void* work, size_t work_bytes, unsigned* d_status,
+                         unsigned long long* d_counters, void* stream);
+
 /* Same computation for callers that cannot allocate device memory (a Fortran
  * or C host program reaching the library through a foreign-function layer
  * with no device allocator, or a service held to a fixed memory budget).  No
@@ -126,6 +138,12 @@ int pg_chi0_mixed_layout(int nb1, int nb2, int nkp, int npb, int omega_batch, in
 size_t pg_eps_inverse_f64_workspace(int npb, int nom);
 int pg_eps_inverse_f64(void* eps, int npb, int nom, void* epsw1, void* epsw2, void* head, void* work,
                        size_t work_bytes, void* stream);
+
+/* Basis change along the leading index of complex arrays (frequency ↔ SVD
+ * basis, pygw.py:3208, 3226, 3276-3280): out[nout][nelem] = in[nin][nelem]·U
+ * with U real (nin, nout), Fortran order, nin·nout ≤ 6144; in ≠ out.  eps
+ * [ω][N][N] has nelem = N·N, the wings [ω][N] nelem = N, the head nelem = 1. */
+int pg_basis_change(const void* in, int nin, void* out, int nout, const double* U, long long nelem, void* stream);
 
 /* ------------------------------------------- ε and ε⁻¹, mixed precision
  * Same contract as pg_eps_inverse_f64 (pygw.py:3229-3271).  The inverse is

@@ -1,7 +1,7 @@
 """numpy restatement of the χ0 contraction and ε⁻¹ (test infrastructure).
 
 Follows MatrixElements2Band.calc_eps (pygw.py:3039-3297) for a Γ-point or
-finite q without the SVD frequency basis:
+finite q, with or without the SVD frequency basis:
 
 * k loop (pygw.py:3083-3200): ``minm2 = reshape(minm, (nb1*nb2, matsiz))``,
   ``tmat = minm2.T*coef * kcw[:nb1,:nb2,ik,iom].ravel()`` (coef = −fspin = −2),
@@ -19,7 +19,11 @@ import numpy as np
 import scipy.linalg
 
 
-def calc_eps(kcw, minm_k, npb, pm_k=None, head=None):
+def calc_eps(kcw, minm_k, npb, pm_k=None, head=None, Ul=None, dUl=None):
+    """With ``Ul`` (nl, nom) and ``dUl`` (nom, nl) — the SVD frequency basis —
+    ``kcw`` holds the par3 weights (nl basis functions) and the flow of
+    pygw.py:3043-3045, 3204-3226, 3274-3280 applies: head, wings and ε to
+    frequencies with Ul before the inverse, back with dUl after it."""
     nb1, nb2, nkp, nom = kcw.shape
     coef = -2.0
     eps = np.zeros((npb, npb, nom), dtype=complex, order="F")
@@ -37,8 +41,15 @@ def calc_eps(kcw, minm_k, npb, pm_k=None, head=None):
             if iq0:
                 epsw1[:, iom] += np.dot(tmat, pm)
     chi0 = eps.copy(order="F")
-    epsw2 = np.conj(epsw1).copy() if iq0 else None
     head = None if head is None else np.array(head, dtype=complex)
+    if Ul is not None:
+        if head is not None:
+            head = np.dot(head, Ul)                       # pygw.py:3044-3045
+        if iq0:
+            epsw1 = np.dot(epsw1, Ul)                     # pygw.py:3206-3208
+        eps = np.dot(eps, Ul)                             # pygw.py:3226
+        nom = eps.shape[2]
+    epsw2 = np.conj(epsw1).copy() if iq0 else None
     Id = np.identity(npb)
     for iom in range(nom):
         eps[:, :, iom] = (eps[:, :, iom] + np.conj(eps[:, :, iom].T)) / 2.0
@@ -54,6 +65,12 @@ def calc_eps(kcw, minm_k, npb, pm_k=None, head=None):
             eps[:, :, iom] += head[iom] * np.tensordot(bw1, w2b, axes=0)
             head[iom] -= 1.0
         eps[:, :, iom] -= Id
+    if dUl is not None:                                   # pygw.py:3274-3280
+        eps = np.dot(eps, dUl)
+        if iq0:
+            epsw1 = np.dot(epsw1, dUl)
+            epsw2 = np.dot(epsw2, dUl)
+            head = np.dot(head, dUl)
     if not iq0:
         return eps, None, None, None, chi0
     return eps, epsw1, epsw2, head, chi0

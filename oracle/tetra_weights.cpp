@@ -5,6 +5,7 @@
 // follow the reference's control flow, thresholds and left-to-right arithmetic:
 //
 //   bz_calcqdepw_par2   for_tetrahedra.f90:390-464   (driver, OpenMP over jb)
+//   bz_calcqdepw_par3   for_tetrahedra.f90:466-542   (the same, weights projected on an SVD frequency basis)
 //   convw1t_par         for_tetrahedra3.f90:3-136    (polyhedron → sub-tets)
 //   genericfunf_par     for_tetrahedra3.f90:139-179  (pentahedron = 2 tets)
 //   genericprism_par    for_tetrahedra3.f90:181-218  (prism = 3 tets)
@@ -1040,6 +1041,73 @@ extern "C" int oracle_bz_calcqdepw_par2(const double* enk, int nbnd, int nkp, do
     stats_out[19] = total.big_weight_zeroed;
   }
   return (int)total.status;
+}
+
+// ------------------------------------------------- bz_calcqdepw_par3
+// for_tetrahedra.f90:466-542: the same loops as par2, but the corner weights
+// of each (tetrahedron, ib, jb) are projected on the SVD frequency basis
+// before they are accumulated: w2t(i,l) = Σ_ω w1t(i,ω)·dUl(ω,l) (matmul,
+// ω ascending), kcw(ib,jb,k,l) += w2t(i,l)·6·wtet.  dUl is (nom, nl) Fortran
+// order; kcw is (ncg+nomx+1, nbnd-ncg-numin, nkp, nl).
+extern "C" int oracle_bz_calcqdepw_par3(const double* enk, int nbnd, int nkp, double ef, const int* kqid, int ncg,
+                                        int nomx, int numin, const double* dUl, int nl, const double* omega, int nom,
+                                        const int* tetc, int ntet, double* kcw, int nthreads) {
+  const int nb1 = ncg + nomx + 1;
+  const int nb2 = nbnd - ncg - numin;
+  if (nb1 <= 0 || nb2 <= 0 || nkp <= 0 || nom <= 0 || ntet <= 0 || nl <= 0 || nom > NOM_MAX || nl > NOM_MAX)
+    return -1;
+  std::vector<int> tetln(ntet);
+  for (int ik = 0; ik < nkp; ik++)
+    for (int it = 1; it <= 6; it++) {
+      int idx = 6 * ik + (it - 1);
+      if (idx < ntet) tetln[idx] = 6 * kqid[ik] + it;
+    }
+  const double wtet = 1.0 / ntet;
+  const size_t nkcw = (size_t)nb1 * nb2 * nkp * nl;
+  for (size_t i = 0; i < nkcw; i++) kcw[i] = 0.0;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  unsigned status = 0;
+  for (int itet = 0; itet < ntet; itet++) {
+    const int lt = tetln[itet] - 1;
+#pragma omp parallel
+    {
+      Stats st;
+      double w1t[4 * NOM_MAX], w2t[4 * NOM_MAX];
+#pragma omp for schedule(static)
+      for (int jb = 1; jb <= nb2; jb++) {
+        double ee2[4], ee1[4];
+        for (int i = 0; i < 4; i++) ee2[i] = enk[(size_t)(jb + ncg + numin - 1) + (size_t)nbnd * tetc[i + 4 * lt]];
+        double mx = ee2[0];
+        for (int i = 1; i < 4; i++) if (ee2[i] > mx) mx = ee2[i];
+        if (mx <= ef) continue;
+        for (int ib = 1; ib <= nb1; ib++) {
+          for (int i = 0; i < 4; i++) ee1[i] = enk[(size_t)(ib - 1) + (size_t)nbnd * tetc[i + 4 * itet]];
+          double mn = ee1[0];
+          for (int i = 1; i < 4; i++) if (ee1[i] < mn) mn = ee1[i];
+          if (mn > ef) continue;
+          convw1t(w1t, ee1, ee2, ef, omega, nom, st);
+          for (int i = 0; i < 4; i++)
+            for (int l = 0; l < nl; l++) {
+              double acc = 0.0;
+              for (int iom = 0; iom < nom; iom++) acc = acc + w1t[i * nom + iom] * dUl[(size_t)iom + (size_t)nom * l];
+              w2t[i * nl + l] = acc;
+            }
+          for (int i = 0; i < 4; i++) {
+            const int kin = tetc[i + 4 * itet];
+            for (int l = 0; l < nl; l++) {
+              double& dst = kcw[(size_t)(ib - 1) + (size_t)nb1 * ((size_t)(jb - 1) + (size_t)nb2 * ((size_t)kin + (size_t)nkp * l))];
+              dst = dst + w2t[i * nl + l] * 6.0 * wtet;
+            }
+          }
+        }
+      }
+#pragma omp critical
+      status |= st.status;
+    }
+  }
+  return (int)status;
 }
 
 // Single tetrahedron entry point (convw1t_par) for known-answer tests.

@@ -4,6 +4,8 @@
 (``kcw = ft.bz_calcqdepw_par2(enk, ef, kqid, ncg, nomx, numin, omega, tetc)``,
 pygw.py:3443, for_tetrahedra.f90:390): array sizes are inferred from the
 shapes, arrays are Fortran-ordered, ``kqid``/``tetc`` are 0-based.
+``bz_calcqdepw_par3`` mirrors ``ft.bz_calcqdepw_par3(enk, ef, kqid, ncg, nomx,
+numin, dUl, omega, tetc)`` (pygw.py:3441, for_tetrahedra.f90:466).
 """
 from __future__ import annotations
 
@@ -31,6 +33,10 @@ def _lib(libm=False):
                                                  ctypes.c_int, ctypes.c_int, dp, ctypes.c_int, ip, ctypes.c_int, dp,
                                                  ctypes.c_int, lp]
         lib.oracle_bz_calcqdepw_par2.restype = ctypes.c_int
+        lib.oracle_bz_calcqdepw_par3.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ip, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_int, dp, ctypes.c_int, dp, ctypes.c_int, ip,
+                                                 ctypes.c_int, dp, ctypes.c_int]
+        lib.oracle_bz_calcqdepw_par3.restype = ctypes.c_int
         lib.oracle_convw1t.argtypes = [dp, dp, ctypes.c_double, dp, ctypes.c_int, dp, lp]
         lib.oracle_convw1t.restype = ctypes.c_int
         lib.oracle_generictetra.argtypes = [dp, dp, dp, dp, ctypes.c_int, dp]
@@ -68,6 +74,28 @@ def bz_calcqdepw_par2(enk, ef, kqid, ncg, nomx, numin, omega, tetc, nthreads=0, 
         raise ValueError("oracle_bz_calcqdepw_par2: bad sizes")
     if return_stats:
         return kcw, int(st), dict(zip(STAT_NAMES, stats.tolist()))
+    return kcw
+
+
+def bz_calcqdepw_par3(enk, ef, kqid, ncg, nomx, numin, dUl, omega, tetc, nthreads=0, libm=False):
+    """Restated SVD-basis weights (for_tetrahedra.f90:466-542); ``dUl[nom, nl]``;
+    returns ``kcw[ncg+nomx+1, nbnd-ncg-numin, nkp, nl]`` (F order)."""
+    enk = np.asfortranarray(enk, dtype=np.float64)
+    kqid = np.ascontiguousarray(kqid, dtype=np.int32)
+    omega = np.ascontiguousarray(omega, dtype=np.float64)
+    tetc = np.asfortranarray(tetc, dtype=np.int32)
+    dUl = np.asfortranarray(dUl, dtype=np.float64)
+    nbnd, nkp = enk.shape
+    nom, nl = dUl.shape
+    if nom != omega.shape[0]:
+        raise ValueError("dUl must be (nom, nl)")
+    ntet = tetc.shape[1]
+    nb1, nb2 = ncg + nomx + 1, nbnd - ncg - numin
+    kcw = np.zeros((nb1, nb2, nkp, nl), order="F")
+    st = _lib(libm).oracle_bz_calcqdepw_par3(_dp(enk), nbnd, nkp, float(ef), _ip(kqid), ncg, nomx, numin, _dp(dUl),
+                                             nl, _dp(omega), nom, _ip(tetc), ntet, _dp(kcw), int(nthreads))
+    if st < 0:
+        raise ValueError("oracle_bz_calcqdepw_par3: bad sizes")
     return kcw
 
 

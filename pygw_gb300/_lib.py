@@ -40,6 +40,11 @@ SIGNATURES = {
                                          c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "pg_synth_minm": (c_int, [c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_int, c_void_p,
                               c_void_p, c_longlong, c_void_p, c_int, ctypes.c_ulonglong, c_void_p, c_void_p]),
+    "pg_bz_calcqdepw_par3_workspace": (c_size_t, [c_int] * 8),
+    "pg_bz_calcqdepw_par3": (c_int, [c_void_p, c_int, c_int, c_double, c_void_p, c_int, c_int, c_int, c_void_p, c_int,
+                                     c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p, c_size_t, c_void_p,
+                                     c_void_p, c_void_p]),
+    "pg_basis_change": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_longlong, c_void_p]),
     "pg_chi0_mixed_layout": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
     "pg_wings_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_int, c_int, c_int, c_double,
                              c_void_p, c_void_p, c_void_p]),

@@ -237,6 +237,27 @@ void launch_finish(double2* eps, int N, int nom, double2* epsw1, double2* epsw2,
   pg_count_launches(1);
 }
 
+// out[j][e] = Σ_i in[i][e]·U[i + nin·j]: complex arrays whose leading index is
+// a frequency or SVD-basis index, transformed by a real (nin, nout) matrix
+// (the basis changes dot(eps, Ul) and dot(eps, dUl) of pygw.py:3226, 3276-3280).
+__global__ void k_basis_change(const double2* __restrict__ in, int nin, double2* __restrict__ out, int nout,
+                               const double* __restrict__ U, long long nelem) {
+  extern __shared__ double us[];
+  for (int i = threadIdx.x; i < nin * nout; i += blockDim.x) us[i] = U[i];
+  __syncthreads();
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nelem) return;
+  for (int j = 0; j < nout; j++) {
+    double re = 0.0, im = 0.0;
+    for (int i = 0; i < nin; i++) {
+      const double2 v = in[(size_t)i * nelem + e];
+      re += v.x * us[i + nin * j];
+      im += v.y * us[i + nin * j];
+    }
+    out[(size_t)j * nelem + e] = make_double2(re, im);
+  }
+}
+
 }  // namespace pge
 
 using namespace pge;
@@ -275,5 +296,17 @@ extern "C" int pg_eps_inverse_f64(void* eps_, int npb, int nom, void* epsw1_, vo
   k_gj_unpermute<<<nom, 256, 0, s>>>(eps, N, perm);
   pg_count_launches(1 + 3ull * N);
   launch_finish(eps, N, nom, q0 ? (double2*)epsw1_ : nullptr, (double2*)epsw2_, (double2*)head_, bw1, w2b, s);
+  return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ECUDA;
+}
+
+// Basis change along the leading (frequency / SVD) index: out[nout][nelem] =
+// in[nin][nelem] · U, U real (nin, nout) Fortran order (device); in ≠ out.
+extern "C" int pg_basis_change(const void* in, int nin, void* out, int nout, const double* U, long long nelem,
+                               void* stream) {
+  if (!in || !out || !U || nin <= 0 || nout <= 0 || nelem <= 0 || in == out) return PG_EARG;
+  if ((size_t)nin * nout * sizeof(double) > 48 * 1024) return PG_ETOOBIG;
+  k_basis_change<<<(unsigned)((nelem + 127) / 128), 128, (size_t)nin * nout * sizeof(double), (cudaStream_t)stream>>>(
+      (const double2*)in, nin, (double2*)out, nout, U, nelem);
+  pg_count_launches(1);
   return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ECUDA;
 }

@@ -1150,6 +1150,28 @@ __global__ void k_gather(const double* scratch, const int* kptr, const int* kslo
   kcw[(size_t)pair + (size_t)P * ((size_t)k + (size_t)nkp * (om0 + w))] = acc;
 }
 
+// ------------------------------------------------------ SVD projection
+// par3 (for_tetrahedra.f90:505-513): every (tetrahedron, corner, pair) weight
+// vector over ω projected on the SVD basis, w2(l) = Σ_ω w1(ω)·dUl(ω,l), ω
+// ascending (the oracle's matmul order; no contraction: -fmad=false).
+// dUl (nom, nl) Fortran order is staged in shared memory.
+__global__ void k_svd_project(const double* __restrict__ scratch, const double* __restrict__ dUl, int nom, int nl,
+                              int P, long long nslot, double* __restrict__ scratch2) {
+  extern __shared__ double du[];
+  for (int i = threadIdx.x; i < nom * nl; i += blockDim.x) du[i] = dUl[i];
+  __syncthreads();
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;   // (slot, pair), slot = 4·tet + corner
+  if (t >= nslot * P) return;
+  const long long slot = t / P;
+  const int pair = (int)(t - slot * P);
+  const double* src = scratch + (size_t)slot * nom * P + pair;
+  for (int l = 0; l < nl; l++) {
+    double acc = 0.0;
+    for (int w = 0; w < nom; w++) acc = acc + src[(size_t)w * P] * du[w + nom * l];
+    scratch2[((size_t)slot * nl + l) * P + pair] = acc;
+  }
+}
+
 }  // namespace pgw
 
 // -------------------------------------------------------------- C-ABI part
@@ -1222,6 +1244,68 @@ extern "C" int pg_bz_calcqdepw_par2(const double* enk, int nbnd, int nkp, double
     k_gather<<<g, 128, 0, s>>>(scratch, kptr, kslot, P, nkp, p.nomc, om0, wtet, kcw);
     pg_count_launches(2);
   }
+  cudaError_t err = cudaGetLastError();
+  return err == cudaSuccess ? PG_OK : PG_ECUDA;
+}
+
+// ---------------------------------------------------------------------------
+// SVD-basis weights (bz_calcqdepw_par3, for_tetrahedra.f90:466-542).
+extern "C" size_t pg_bz_calcqdepw_par3_workspace(int nbnd, int nkp, int ncg, int nomx, int numin, int nom, int ntet,
+                                                  int nl) {
+  const long long nb1 = ncg + nomx + 1, nb2 = nbnd - ncg - numin;
+  if (nb1 <= 0 || nb2 <= 0 || nkp <= 0 || ntet <= 0 || nom <= 0 || nl <= 0) return 0;
+  return lists_bytes(nkp, ntet, nb1 * nb2 * ntet) + align256(sizeof(double) * (size_t)4 * ntet * nom * nb1 * nb2) +
+         align256(sizeof(double) * (size_t)4 * ntet * nl * nb1 * nb2);
+}
+
+// kcw (nb1, nb2, nkp, nl) = the par2 corner weights of every (tetrahedron,
+// pair) projected on dUl (device, (nom, nl) Fortran order) and accumulated
+// like par2.  All frequencies are evaluated in one pass.
+extern "C" int pg_bz_calcqdepw_par3(const double* enk, int nbnd, int nkp, double ef, const int* kqid, int ncg,
+                                    int nomx, int numin, const double* dUl, int nl, const double* omega, int nom,
+                                    const int* tetc, int ntet, double* kcw, void* work, size_t work_bytes,
+                                    unsigned* d_status, unsigned long long* d_counters, void* stream) {
+  const int nb1 = ncg + nomx + 1, nb2 = nbnd - ncg - numin;
+  if (!enk || !kqid || !omega || !tetc || !kcw || !work || !dUl) return PG_EARG;
+  if (nb1 <= 0 || nb2 <= 0 || nkp <= 0 || ntet <= 0 || nom <= 0 || nl <= 0 || ncg < 0 || numin < 0) return PG_EARG;
+  if (ntet != 6 * nkp) return PG_EARG;
+  if ((size_t)nom * nl * sizeof(double) > 48 * 1024) return PG_ETOOBIG;   // dUl staged in shared memory
+  const long long items = (long long)nb1 * nb2 * ntet;
+  if (items >= (1ll << 31)) return PG_ETOOBIG;
+  if (work_bytes < pg_bz_calcqdepw_par3_workspace(nbnd, nkp, ncg, nomx, numin, nom, ntet, nl)) return PG_EWORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  char* w = (char*)work;
+  int* kptr = (int*)w; w += align256(sizeof(int) * (size_t)(nkp + 1));
+  int* kcount = (int*)w; w += align256(sizeof(int) * (size_t)nkp);
+  int* kslot = (int*)w; w += align256(sizeof(int) * (size_t)4 * ntet);
+  unsigned char* cls = (unsigned char*)w; w += align256((size_t)items);
+  int* order = (int*)w; w += align256(sizeof(int) * (size_t)items);
+  unsigned* hist = (unsigned*)w; w += align256(sizeof(unsigned) * NCLASS);
+  unsigned* cursor = (unsigned*)w; w += align256(sizeof(unsigned) * NCLASS);
+  double* scratch = (double*)w; w += align256(sizeof(double) * (size_t)4 * ntet * nom * nb1 * nb2);
+  double* scratch2 = (double*)w;
+  k_kcsr_count<<<(nkp + 127) / 128, 128, 0, s>>>(tetc, ntet, nkp, kcount);
+  k_kcsr_scan<<<1, 1, 0, s>>>(kcount, nkp, kptr);
+  k_kcsr_fill<<<(nkp + 127) / 128, 128, 0, s>>>(tetc, ntet, nkp, kptr, kslot);
+  const int P = nb1 * nb2;
+  Params p;
+  p.enk = enk; p.kqid = kqid; p.omega = omega; p.tetc = tetc; p.scratch = scratch; p.order = nullptr;
+  p.status = d_status; p.counters = d_counters; p.ef = ef;
+  p.nbnd = nbnd; p.nkp = nkp; p.ncg = ncg; p.numin = numin; p.nb1 = nb1; p.nb2 = nb2; p.ntet = ntet;
+  p.om0 = 0; p.nomc = nom;
+  const unsigned nblk = (unsigned)((items + 127) / 128);
+  if (cudaMemsetAsync(hist, 0, sizeof(unsigned) * NCLASS, s) != cudaSuccess) return PG_ECUDA;
+  k_tet_classify<<<nblk, 128, 0, s>>>(p, items, cls, hist);
+  k_class_offsets<<<1, 32, 0, s>>>(hist, cursor);
+  k_class_scatter<<<nblk, 128, 0, s>>>(cls, items, cursor, order);
+  p.order = order;
+  k_tet_weights<<<nblk, 128, 0, s>>>(p);
+  const long long nthr = (long long)4 * ntet * P;
+  k_svd_project<<<(unsigned)((nthr + 127) / 128), 128, (size_t)nom * nl * sizeof(double), s>>>(
+      scratch, dUl, nom, nl, P, (long long)4 * ntet, scratch2);
+  dim3 g((P + 127) / 128, nkp, nl);
+  k_gather<<<g, 128, 0, s>>>(scratch2, kptr, kslot, P, nkp, nl, 0, 1.0 / ntet, kcw);
+  pg_count_launches(10);
   cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? PG_OK : PG_ECUDA;
 }

@@ -314,24 +314,47 @@ def eps_inverse(eps, npb, nom, epsw1=None, head=None, stream=None, precision=Non
 
 
 def chi0_eps(kcw, minm, nkp, npb, nb1, nb2, nom, pm_k=None, head=None, k_chunk=None, stream=None, precision=None,
-             timers=None):
+             timers=None, Ul=None, dUl=None):
     """The whole ε path for one q on the GPU: returns an ``EpsResult``.
 
-    ``minm``: per-k callable or ``[nkp, P, npb]`` tensor (see chi0_accumulate)."""
+    ``minm``: per-k callable or ``[nkp, P, npb]`` tensor (see chi0_accumulate).
+    With the SVD frequency basis (``Ul`` (nl, nω), ``dUl`` (nω, nl)), ``kcw``
+    holds par3 weights, ``nom`` is nl and ``head`` is given in the basis; χ0 is
+    accumulated on the nl basis functions, ε, its wings and head go to
+    frequencies with Ul for the inverse and back with dUl (pygw.py:3043-3045,
+    3204-3226, 3274-3280)."""
     require_cuda()
     kcw_d = _kcw_device(kcw)
     precision = precision or PRECISION
+    status = None
     if precision == "mixed":
         status = torch.zeros(1, dtype=torch.int32, device="cuda")
         eps, epsw1 = chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=pm_k, k_chunk=k_chunk, stream=stream,
                                      precision="mixed", timers=timers, status=status)
-        r = eps_inverse(eps, npb, nom, epsw1=epsw1, head=head, stream=stream, precision="mixed")
+    else:
+        eps, epsw1 = chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=pm_k, k_chunk=k_chunk, stream=stream,
+                                     precision=precision, timers=timers)
+        chi0_finalize(eps, npb, nom, stream=stream, precision=precision)
+    if Ul is None:
+        r = eps_inverse(eps, npb, nom, epsw1=epsw1, head=head, stream=stream, precision=precision)
         r.chi0_status = status
         return r
-    eps, epsw1 = chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=pm_k, k_chunk=k_chunk, stream=stream,
-                                 precision=precision, timers=timers)
-    chi0_finalize(eps, npb, nom, stream=stream, precision=precision)
-    return eps_inverse(eps, npb, nom, epsw1=epsw1, head=head, stream=stream, precision=precision)
+    from .svd import to_basis
+    Ul = np.asarray(Ul, dtype=np.float64)
+    dUl = np.asarray(dUl, dtype=np.float64)
+    eps_w = to_basis(eps, Ul, stream=stream)
+    epsw1_w = to_basis(epsw1, Ul, stream=stream) if epsw1 is not None else None
+    head_w = None if head is None else np.dot(np.asarray(head, dtype=complex), Ul)
+    nw = Ul.shape[1]
+    r = eps_inverse(eps_w, npb, nw, epsw1=epsw1_w, head=head_w, stream=stream, precision=precision)
+    out = EpsResult(to_basis(r.eps, dUl, stream=stream),
+                    to_basis(r.epsw1, dUl, stream=stream) if r.epsw1 is not None else None,
+                    to_basis(r.epsw2, dUl, stream=stream) if r.epsw2 is not None else None,
+                    to_basis(r.head.reshape(nw, 1), dUl, stream=stream).reshape(-1) if r.head is not None else None,
+                    npb, Ul.shape[0])
+    out.status = r.status
+    out.chi0_status = status
+    return out
 
 
 class MatrixElements2Band:
@@ -349,12 +372,11 @@ class MatrixElements2Band:
 
     def calc_eps(self, iq, head_quantities, strc, in1, latgen, kqm, ks, radf, pw, pb, core, kw, fr, kcw, ddir, dUl,
                  Ul, fout):
-        if dUl is not None or Ul is not None:
-            raise NotImplementedError("SVD frequency basis: not part of this branch yet")
         nvbm, ncbm = ks.nomax_numin[0] + 1, ks.nomax_numin[1]
         nb1, nb2 = ks.ncg_p + nvbm, ks.nbmaxpol - ncbm
         nkp = len(kqm.kii_ind)
-        nom = len(fr.omega)
+        # with the SVD basis kcw (par3) and the outputs carry nl basis functions
+        nom = len(fr.omega) if Ul is None else np.asarray(Ul).shape[0]
         band_limits = (0, nvbm, ncbm, ks.nbmaxpol, 0, ks.ncg_p)
 
         def minm_k(ik):
@@ -365,9 +387,9 @@ class MatrixElements2Band:
         if iq == 0:
             head = head_quantities[0]
             pm_k = self.pm_k
-        r = chi0_eps(kcw, minm_k, nkp, self.matsize, nb1, nb2, nom, pm_k=pm_k, head=head)
+        r = chi0_eps(kcw, minm_k, nkp, self.matsize, nb1, nb2, nom, pm_k=pm_k, head=head, Ul=Ul, dUl=dUl)
         eps, epsw1, epsw2, head_out = r.numpy()
         if fout is not None:
-            for iom in range(nom):
+            for iom in range(eps.shape[2]):
                 print("Tr(1/eps[%3d]-1) = %18.14f" % (iom + 1, np.trace(eps[:, :, iom]).real), file=fout)
         return eps, epsw1, epsw2, head_out
