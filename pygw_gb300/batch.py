@@ -47,6 +47,9 @@ class QTask:
     npb: int
     sqv: np.ndarray                      # √v_I, length npb
     knb2: np.ndarray | None = None       # per-k unoccupied bands in the window (None: all nb2)
+    pm: np.ndarray | None = None         # q → 0: wing vectors [nkp][nb1·nb2] (full window only)
+    head: np.ndarray | None = None       # q → 0: head [nom] (FP64 complex); None with pm: the synthetic
+    #                                      head −2 Σ_k Σ_p |pm|²·w from this q's weights, formed on the device
 
 
 @dataclass
@@ -121,8 +124,30 @@ class Batch:
         self.om_d = torch.from_numpy(self.omega.copy()).cuda()
         self.sqv_d = [torch.from_numpy(np.asarray(t.sqv, dtype=np.float64)).cuda() for t in self.tasks]
         self.kcw = torch.empty((self.nom, self.nkp, self.nb2, self.nb1), dtype=torch.float64, device="cuda")
-        wbytes = self.lib.pg_bz_calcqdepw_par2_workspace(self.nbnd, self.nkp, ncg, nomx, numin, self.nom, self.ntet, 0)
+        # weight scratch: all frequencies at once unless that exceeds a quarter of the free memory
+        free0, _ = torch.cuda.mem_get_info()
+        self.nom_chunk = self.nom
+        while self.nom_chunk > 1 and self.lib.pg_bz_calcqdepw_par2_workspace(
+                self.nbnd, self.nkp, ncg, nomx, numin, self.nom, self.ntet, self.nom_chunk) > free0 // 4:
+            self.nom_chunk = (self.nom_chunk + 1) // 2
+        wbytes = self.lib.pg_bz_calcqdepw_par2_workspace(self.nbnd, self.nkp, ncg, nomx, numin, self.nom, self.ntet,
+                                                         self.nom_chunk)
         self.wwork = torch.empty(wbytes, dtype=torch.uint8, device="cuda")
+        # q → 0: wings and head (uniform windows)
+        self.q0 = {}
+        for i, t in enumerate(self.tasks):
+            if t.pm is None:
+                continue
+            if t.knb2 is not None and np.any(np.asarray(t.knb2) < self.nb2):
+                raise ValueError("q → 0 wings need the full band window")
+            self.q0[i] = {"pm": torch.from_numpy(np.ascontiguousarray(t.pm, dtype=np.complex128)).cuda(),
+                          "head0": (None if t.head is None else
+                                    torch.from_numpy(np.asarray(t.head, dtype=np.complex128).copy()).cuda()),
+                          "pm2": torch.from_numpy(np.abs(np.asarray(t.pm)) ** 2).cuda(),
+                          "head": torch.empty(self.nom, dtype=torch.complex128, device="cuda"),
+                          "hre": torch.empty(self.nom, dtype=torch.float64, device="cuda"),
+                          "w1": torch.empty((self.nom, t.npb), dtype=torch.complex128, device="cuda"),
+                          "w2": torch.empty((self.nom, t.npb), dtype=torch.complex128, device="cuda")}
         self.wstatus = torch.zeros(len(self.tasks), dtype=torch.int32, device="cuda")
         # per-q window bookkeeping
         self.knb2 = [np.full(self.nkp, self.nb2, dtype=np.int32) if t.knb2 is None
@@ -207,7 +232,7 @@ class Batch:
         rc = self.lib.pg_bz_calcqdepw_par2(ptr(self.enk_d), self.nbnd, self.nkp, self.ef, ptr(self.kqid_d[t.iq]),
                                            self.ncg, self.nomx, self.numin, ptr(self.om_d), self.nom,
                                            ptr(self.tetc_d), self.ntet, ptr(self.kcw), ptr(self.wwork),
-                                           self.wwork.numel(), 0, ptr(self.wstatus[i:i + 1]), None, sh)
+                                           self.wwork.numel(), self.nom_chunk, ptr(self.wstatus[i:i + 1]), None, sh)
         self._check(rc, "pg_bz_calcqdepw_par2")
 
     def _chi0(self, i, sh, nom, chunks, wb, eps):
@@ -224,6 +249,11 @@ class Batch:
                                                    ptr(self.cwork), self.cwork.numel(), wb, 0,
                                                    ptr(self.cstatus[i:i + 1]), sh, None)
             self._check(rc, "pg_chi0_mixed_accumulate")
+            if i in self.q0 and eps is self.results[i]:
+                q = self.q0[i]
+                rc = self.lib.pg_wings_f64(ptr(mv), kc, k0, ptr(self.kcw), self.nb1, self.nb2, self.nkp, nom, N,
+                                           -FSPIN, ptr(q["pm"][k0:k0 + kc]), ptr(q["w1"]), sh)
+                self._check(rc, "pg_wings_f64")
 
     def enqueue(self):
         """All launches of the batch on the current stream (no host synchronisation)."""
@@ -233,9 +263,23 @@ class Batch:
             self._weights(i, sh)
             c = self.choice[i]
             eps = self.results[i]
+            q = self.q0.get(i)
+            if q is not None:
+                q["w1"].zero_()
+                if q["head0"] is not None:
+                    q["head"].copy_(q["head0"])
+                else:
+                    # synthetic head from the weights: kcw [ω][k][m][n] → pair n·nb2 + m as pm
+                    w = self.kcw.permute(0, 1, 3, 2).reshape(self.nom, self.nkp, -1)
+                    torch.mul(torch.einsum("wkp,kp->w", w, q["pm2"]), -2.0, out=q["hre"])
+                    q["head"].copy_(q["hre"])
             self._chi0(i, sh, self.nom, self.kstart_d[i], c.omega_batch, eps)
-            rc = self.lib.pg_eps_inverse_mixed(ptr(eps), t.npb, self.nom, None, None, None, ptr(self.ework),
-                                               self.ework.numel(), 0, int(iters), ptr(self.estatus[i:i + 1]), sh)
+            if q is not None:
+                torch.conj_physical(q["w1"], out=q["w2"])
+            rc = self.lib.pg_eps_inverse_mixed(ptr(eps), t.npb, self.nom, ptr(q["w1"]) if q else None,
+                                               ptr(q["w2"]) if q else None, ptr(q["head"]) if q else None,
+                                               ptr(self.ework), self.ework.numel(), 0, int(iters),
+                                               ptr(self.estatus[i:i + 1]), sh)
             self._check(rc, "pg_eps_inverse_mixed")
 
     def capture(self):
@@ -326,3 +370,18 @@ def batch_for(problem, tasks, **kw):
     nomx, numin = b.nomax_numin
     return Batch(b.enk(), b.EF, problem.kqm.kqid, problem.kqm.tetc, b.ncg_p, nomx, numin, problem.fr.omega, tasks,
                  seed=problem.w.seed, **kw)
+
+
+def c5_tasks(problem):
+    """The large workload's q list: full band windows, the first q is Γ (q → 0)
+    with synthetic wing vectors and the head formed from its weights."""
+    from . import synthetic as syn
+    w = problem.w
+    b = problem.bands
+    tasks = []
+    for iq in problem.qs:
+        t = QTask(iq=iq, npb=w.npb, sqv=syn.coulomb_sqrt(w, iq, w.npb))
+        if iq == 0:
+            t.pm = np.stack([syn.pm_k(w, b, ik) for ik in range(problem.kqm.nkp)])
+        tasks.append(t)
+    return tasks

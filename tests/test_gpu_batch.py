@@ -52,3 +52,28 @@ def test_batch_uneven_q_matches_oracle_and_graph_equals_eager():
         rel = max(np.max(np.abs(got[..., o] - ref[..., o])) / np.max(np.abs(ref[..., o] + np.eye(n)))
                   for o in range(w.nom))
         assert rel < 1e-9, (i, t.npb, rel)
+
+
+def test_batch_q0_wings_and_head_match_oracle():
+    """The large workload's q list at a small size: q = Γ with wings and the
+    head formed from its weights on the device, against the FP64 oracle."""
+    w = syn.scaled(syn.WORKLOADS["C5"], div=3, nbands=36, nocc=6, npb=96, nom=5, nq=2)
+    prob = syn.Problem(w)
+    b = prob.bands
+    tasks = pb.c5_tasks(prob)
+    assert tasks[0].iq == 0 and tasks[0].pm is not None
+    bt = pb.batch_for(prob, tasks)
+    bt.run(graph=True)
+    assert bt.status() == 0
+    nomx, numin = b.nomax_numin
+    t = tasks[0]
+    kcw = ow.bz_calcqdepw_par2(b.enk(), b.EF, prob.kqm.kqid[:, 0], 0, nomx, numin, prob.fr.omega, prob.kqm.tetc)
+    m = _matrix_elements(bt, 0, b.nb1, b.nb2)
+    pms = [t.pm[ik] for ik in range(bt.nkp)]
+    head = syn.head_from_weights(kcw, pms)
+    ref = oe.calc_eps(kcw, lambda ik: m[ik], t.npb, pm_k=lambda ik: pms[ik], head=head)
+    got = bt.results[0].cpu().numpy().transpose(2, 1, 0)
+    q = bt.q0[0]
+    for a, e in ((got, ref[0]), (q["w1"].cpu().numpy().T, ref[1]), (q["w2"].cpu().numpy().T, ref[2]),
+                 (q["head"].cpu().numpy(), ref[3])):
+        assert np.max(np.abs(a - e)) <= 1e-9 * max(1.0, np.max(np.abs(e)))
