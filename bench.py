@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--div", type=int, default=0, help="override the k-mesh divisions (smaller profiling case)")
     ap.add_argument("--npb", type=int, default=0, help="override the product-basis size (smaller profiling case)")
+    ap.add_argument("--q-limit", type=int, default=0, help="batched workloads: only the first n q points")
+    ap.add_argument("--no-tune", action="store_true", help="batched workloads: default work split, no autotuning")
+    ap.add_argument("--no-graph", action="store_true", help="batched workloads: enqueue eagerly, no CUDA graph")
     return ap.parse_args()
 
 
@@ -346,8 +349,10 @@ def run_reference(a, w, rank):
 
 # ------------------------------------------------------- batched workload
 def run_batch_workload(a, w, rank, world, sampler):
-    """C4: the q points of uneven N_PB (and ragged per-k windows) as one
-    captured CUDA graph per step; value = step time / q points of the step."""
+    """C4 (q points of uneven N_PB and ragged per-k windows) and C5 (matrix
+    elements too large to hold: drawn per k-chunk on the device; q = Γ with
+    head and wings) through the batch driver, one captured CUDA graph per step
+    unless --no-graph; value = step time / q points of the step."""
     import torch
     from pygw_gb300 import _lib
     from pygw_gb300 import batch as pb
@@ -356,22 +361,29 @@ def run_batch_workload(a, w, rank, world, sampler):
     from pygw_gb300.device import ptr, stream_handle
     lib = _lib.load()
     prob = syn.Problem(w)
-    tasks = pb.c4_tasks(prob)[rank::world]
+    tasks = (pb.c5_tasks(prob) if not w.npb_range else pb.c4_tasks(prob))
+    if a.q_limit:
+        tasks = tasks[:a.q_limit]
+    tasks = tasks[rank::world]
     t0 = time.time()
-    tuner = pb.Tuner(path=os.path.join(ROOT, "gpurun_out", "tune_c4.json") if os.path.isdir(
-        os.path.join(ROOT, "gpurun_out")) else None)
+    tuner = None if a.no_tune else pb.Tuner(path=os.path.join(ROOT, "gpurun_out", f"tune_{w.name}.json")
+                                           if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else None)
     bt = pb.batch_for(prob, tasks, tuner=tuner)
-    bt.capture()
+    graph = not a.no_graph
+    if graph:
+        bt.capture()
     setup_s = time.time() - t0
     stream = torch.cuda.current_stream()
+    l0 = lib.pg_launch_count()
     for _ in range(a.warmup):
-        bt.run(graph=True)
+        bt.run(graph=graph)
     torch.cuda.synchronize()
+    per_run = bt.graph_launches if graph else (lib.pg_launch_count() - l0) // max(1, a.warmup)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     wall0 = time.time()
     ev0.record(stream)
     for _ in range(a.steps):
-        bt.run(graph=True)
+        bt.run(graph=graph)
     ev1.record(stream)
     torch.cuda.synchronize()
     wall1 = time.time()
@@ -435,7 +447,7 @@ def run_batch_workload(a, w, rank, world, sampler):
             bt.enk_d.copy_(host_in[0], non_blocking=True)
             bt.tetc_d.copy_(host_in[1], non_blocking=True)
             bt.om_d.copy_(host_in[2], non_blocking=True)
-            bt.run(graph=True)
+            bt.run(graph=graph)
             for o, r in zip(outs, bt.results):
                 o.copy_(r, non_blocking=True)
         torch.cuda.synchronize()
@@ -451,14 +463,16 @@ def run_batch_workload(a, w, rank, world, sampler):
                 "unit": "s/q-point", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
                 "ms_per_step": dt / a.steps * 1e3, "higher_is_better": False, "scaling": "weak",
                 "vs_baseline": None, "dtype": "bf16-digits/f32-exact/f64", "data": "synthetic",
-                "config": {"workload": workload_desc(w) + f", N_PB per q {[t.npb for t in tasks]}, per-k "
-                                                          f"unoccupied cutoff 100-300 bands",
+                "config": {"workload": workload_desc(w) + f", N_PB per q {[t.npb for t in tasks]}"
+                                                          + (", per-k unoccupied cutoff 100-300 bands" if w.npb_range
+                                                             else f", q {[t.iq for t in tasks]} (q=0: head and "
+                                                                  f"wings)"),
                            "precision": "mixed", "parallelism": "replicas",
-                           "batch": {"q_per_step": nq, "graph": True, "setup_s": setup_s,
+                           "batch": {"q_per_step": nq, "graph": graph, "setup_s": setup_s,
                                      "tuned": [[c.k_chunk, c.omega_batch] for c in bt.choice]},
                            "l2": "inputs larger than L2 (matrix elements drawn per k-chunk on the device)"},
                 "roofline": roof, "kernel_status": status, "fp64_gpu": fp64, "cpu_baseline": None,
-                "e2e": e2e, "gpu_launches": int(bt.graph_launches * a.steps), "clocks": clocks}
+                "e2e": e2e, "gpu_launches": int(per_run * a.steps), "clocks": clocks}
         print(json.dumps(line), flush=True)
 
 
@@ -489,7 +503,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from pygw_gb300 import _lib
 
-    if w.npb_range:
+    if w.npb_range or w.name == "C5":
         return run_batch_workload(a, w, rank, world, sampler)
     lib = _lib.load()
     inp = Inputs(w, rank)
