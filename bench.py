@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--q-limit", type=int, default=0, help="batched workloads: only the first n q points")
     ap.add_argument("--no-tune", action="store_true", help="batched workloads: default work split, no autotuning")
     ap.add_argument("--no-graph", action="store_true", help="batched workloads: enqueue eagerly, no CUDA graph")
+    ap.add_argument("--tune-file", default=None, help="batched workloads: JSON file the autotuner reads and extends")
     return ap.parse_args()
 
 
@@ -272,8 +273,8 @@ def mixed_tile_area(npb):
 
 
 # GB300's FP64 rate (CUDA cores; it has no faster FP64 tensor path).  The
-# measured peaks file holds HBM and bf16 figures only, so the FP64
-# roofline of the plain path is quoted against this nominal figure.
+# measured peaks file holds HBM and bf16 figures only, so the FP64 roofline
+# of the plain path is quoted against this nominal figure.
 FP64_NOMINAL_TFLOPS = 1.25
 
 
@@ -366,8 +367,7 @@ def run_batch_workload(a, w, rank, world, sampler):
         tasks = tasks[:a.q_limit]
     tasks = tasks[rank::world]
     t0 = time.time()
-    tuner = None if a.no_tune else pb.Tuner(path=os.path.join(ROOT, "gpurun_out", f"tune_{w.name}.json")
-                                           if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else None)
+    tuner = None if a.no_tune else pb.Tuner(path=a.tune_file)
     bt = pb.batch_for(prob, tasks, tuner=tuner)
     graph = not a.no_graph
     if graph:
