@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--div", type=int, default=0, help="override the k-mesh divisions (smaller profiling case)")
     ap.add_argument("--npb", type=int, default=0, help="override the product-basis size (smaller profiling case)")
+    ap.add_argument("--nom", type=int, default=0, help="override the number of frequencies (smaller profiling case)")
     ap.add_argument("--q-limit", type=int, default=0, help="batched workloads: only the first n q points")
     ap.add_argument("--no-tune", action="store_true", help="batched workloads: default work split, no autotuning")
     ap.add_argument("--no-graph", action="store_true", help="batched workloads: enqueue eagerly, no CUDA graph")
@@ -483,8 +484,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     from pygw_gb300.synthetic import WORKLOADS, scaled
     w = WORKLOADS[a.workload]
-    if a.div or a.npb:
-        w = scaled(w, div=a.div or w.div, npb=a.npb or w.npb)
+    if a.div or a.npb or a.nom:
+        w = scaled(w, div=a.div or w.div, npb=a.npb or w.npb, nom=a.nom or w.nom)
     if a.impl == "reference":
         return run_reference(a, w, rank)
 
