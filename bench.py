@@ -366,7 +366,8 @@ def run_batch_workload(a, w, rank, world, sampler):
     tasks = (pb.c5_tasks(prob) if not w.npb_range else pb.c4_tasks(prob))
     if a.q_limit:
         tasks = tasks[:a.q_limit]
-    tasks = tasks[rank::world]
+    from pygw_gb300 import replicas
+    tasks = replicas.my_points(tasks, rank, world) or tasks[:1]
     t0 = time.time()
     tuner = None if a.no_tune else pb.Tuner(path=a.tune_file)
     bt = pb.batch_for(prob, tasks, tuner=tuner)
@@ -513,8 +514,9 @@ def main():
     if a.precision == "mixed":
         from pygw_gb300 import eps as peps
         inp.wb = peps.mixed_omega_batch(inp.nb1, inp.nb2, inp.nkp, w.npb, w.nom)
-    # replicas: rank r visits q points r, r+world, ... (the reference's q split)
-    inp.qs = inp.qs[rank::world] or inp.qs[:1]
+    # replicas: each rank runs its contiguous block of q points (the reference's mpiSplitArray)
+    from pygw_gb300 import replicas
+    inp.qs = replicas.my_points(inp.qs, rank, world) or inp.qs[:1]
 
     def barrier():
         if dist is not None:
