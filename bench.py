@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--no-tune", action="store_true", help="batched workloads: default work split, no autotuning")
     ap.add_argument("--no-graph", action="store_true", help="batched workloads: enqueue eagerly, no CUDA graph")
     ap.add_argument("--tune-file", default=None, help="batched workloads: JSON file the autotuner reads and extends")
+    ap.add_argument("--path", default="polarization", choices=["polarization", "selfc"],
+                    help="selfc: the correlation self-energy step (mwm contraction + Matsubara convolution) "
+                         "on the workload's k mesh, N_PB and frequencies")
+    ap.add_argument("--selfc-nb1", type=int, default=16, help="selfc: GW bands (nbgw - ibgw)")
     return ap.parse_args()
 
 
@@ -478,6 +482,207 @@ def run_batch_workload(a, w, rank, world, sampler):
         print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------- self-energy
+def run_selfc(a, w, rank, world, sampler):
+    """Seconds per q-point of calc_selfc's GPU body (pygw.py:3335-3385): mwm
+    over every k-point (split precision, or FP64 with --precision fp64) and the
+    Matsubara convolution (all_fr_convolutions).  nb1 = --selfc-nb1 GW bands,
+    nb2 = all bands of the workload, M drawn on the device and resident, ε⁻¹−1
+    a seeded negative semidefinite Hermitian matrix per frequency."""
+    import torch
+    from pygw_gb300 import _lib
+    from pygw_gb300 import selfc as gsc
+    from pygw_gb300 import synthetic as syn
+    from pygw_gb300.device import ptr, stream_handle
+    lib = _lib.load()
+    prob = syn.Problem(w)
+    b = prob.bands
+    kqm = prob.kqm
+    nkp, N, nom = kqm.nkp, w.npb, w.nom
+    enk = b.enk()                                     # [nbnd, nkp]
+    nbnd = enk.shape[0]
+    nb1, nb2 = min(a.selfc_nb1, nbnd), nbnd
+    P = nb1 * nb2
+    from pygw_gb300 import replicas
+    qs = replicas.my_points(list(prob.qs), rank, world) or list(prob.qs[:1])
+    iq = qs[0]
+    enk_d = torch.from_numpy(np.ascontiguousarray(enk.T)).cuda()
+    kq_d = torch.from_numpy(np.ascontiguousarray(kqm.kqid[:, iq].astype(np.int32))).cuda()
+    sqv_d = torch.from_numpy(syn.coulomb_sqrt(w, iq, N)).cuda()
+    M = torch.empty((nkp, P, N), dtype=torch.complex128, device="cuda")
+    _lib.check(lib.pg_synth_minm(nkp, 0, iq, ptr(enk_d), nbnd, ptr(kq_d), 0, 0, nb1, nb2, None, None, 0, ptr(sqv_d),
+                                 N, w.seed, ptr(M), stream_handle(None)), "pg_synth_minm")
+    g = torch.Generator(device="cuda").manual_seed(w.seed)
+    W = torch.empty((nom, N, N), dtype=torch.complex128, device="cuda")
+    for iw in range(nom):                             # ε⁻¹ − 1 ≤ 0, decaying with the frequency
+        B = torch.randn((N, N), dtype=torch.complex128, device="cuda", generator=g)
+        W[iw] = -(B @ B.conj().T) * (0.5 / N / (1.0 + prob.fr.omega[iw]))
+    # k-points at k−q in the energy list of the convolution (no core states here)
+    ekq = np.stack([enk[:, int(kqm.kqid[ik, iq])] for ik in range(nkp)])          # [nkp][nb2]
+    om = prob.fr.omega
+    wom = np.gradient(om)
+    wkq = 1.0 / nkp
+    precision = a.precision
+    budget = 24 << 30
+    k_chunk, nb = gsc.mixed_k_chunk(P, N, nom, budget) if precision == "mixed" else (nkp, nom)
+    k_chunk = min(k_chunk, nkp)
+    workspace_mixed = None
+    if precision == "mixed":
+        workspace_mixed = torch.empty(lib.pg_selfc_mwm_workspace(k_chunk, P, N, nb, 1), dtype=torch.uint8,
+                                      device="cuda")
+    mwm_d = torch.empty((nkp, nom, P), dtype=torch.complex128, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    om_d = torch.from_numpy(om.copy()).cuda()
+    wom_d = torch.from_numpy(wom).cuda()
+    ekq_d = torch.from_numpy(ekq).cuda()
+    sc_d = torch.empty((nkp, nb1, nom), dtype=torch.complex128, device="cuda")
+    stream = torch.cuda.current_stream()
+    sh = stream_handle(None)
+    g_ev = []
+
+    def step(timed=False, phases=None):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)] if phases is not None else None
+        if ev:
+            ev[0].record(stream)
+        for k0 in range(0, nkp, k_chunk):
+            nk = min(k_chunk, nkp - k0)
+            if timed:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            rc = lib.pg_selfc_mwm(ptr(M[k0]), nk, P, N, ptr(W), nom, wkq, ptr(mwm_d[k0]),
+                                  1 if precision == "mixed" else 0, nb, ptr(workspace_mixed),
+                                  0 if workspace_mixed is None else workspace_mixed.numel(), ptr(status), sh)
+            _lib.check(rc, "pg_selfc_mwm")
+            if timed:
+                e1.record(stream)
+                g_ev.append((e0, e1, nk))
+        if ev:
+            ev[1].record(stream)
+        rc = lib.pg_selfc_convolution(ptr(mwm_d), nkp, nb1, nb2, nom, ptr(ekq_d), ptr(om_d), ptr(wom_d), 0, None,
+                                      None, None, None, 0, ptr(sc_d), sh)
+        _lib.check(rc, "pg_selfc_convolution")
+        if ev:
+            ev[2].record(stream)
+            phases.append(ev)
+
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+    phases = []
+    l0 = lib.pg_launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    wall0 = time.time()
+    ev0.record(stream)
+    for _ in range(a.steps):
+        step(timed=True, phases=phases)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    wall1 = time.time()
+    launches = lib.pg_launch_count() - l0
+    dt = ev0.elapsed_time(ev1) * 1e-3
+    value = dt / a.steps
+    phase_ms = {name: statistics.mean(e[i].elapsed_time(e[i + 1]) for e in phases)
+                for i, name in enumerate(["mwm", "convolution"])}
+    # roofline of the contraction: the reference's complex GEMM count 8·P·N²·nω per k-point
+    mw_s = sum(e0.elapsed_time(e1) for e0, e1, _ in g_ev) * 1e-3
+    alg = sum(8.0 * nk * P * N * N * nom for _, _, nk in g_ev)
+    peaks = json.load(open(PEAKS_FILE)) if os.path.exists(PEAKS_FILE) else {}
+    if precision == "mixed":
+        peak = peaks.get("bf16_tflops", 1900.0)
+        note = "of measured" if "bf16_tflops" in peaks else "of fallback"
+        rpad_b = -(-N // 256) * 256
+        kpad = -(-2 * N // 64) * 64
+        exe = sum(15 * 2.0 * (-(-2 * nk * P // 256) * 256) * min(rpad_b, -(-N // 128) * 128) * kpad * nom
+                  for _, _, nk in g_ev)
+        roof = {"kernel": "pg_selfc_mwm (k_rows_digits + per frequency batch: column digits, k_ozaki_gemm general "
+                          "mode, k_mwm_reduce)", "bound": "tensor", "achieved": alg / mw_s / 1e12, "peak": peak,
+                "unit": "TFLOP/s", "frac": alg / mw_s / 1e12 / peak, "traffic": None,
+                "executed_bf16_tflops": exe / mw_s / 1e12, "executed_frac": exe / mw_s / 1e12 / peak,
+                "note": "achieved = 8*P*N^2*Nw per k (the reference's complex matmul count) / CUDA-event time of "
+                        "the contraction calls; executed = 15 digit-pair bf16 products of the (2R x 2N)(2N x N) "
+                        "real form; peak = bf16 " + note}
+    else:
+        peak = FP64_NOMINAL_TFLOPS
+        roof = {"kernel": "k_mwm_f64", "bound": "fp64", "achieved": alg / mw_s / 1e12, "peak": peak,
+                "unit": "TFLOP/s", "frac": alg / mw_s / 1e12 / peak, "traffic": None,
+                "note": "peak = nominal GB300 FP64 (no measured FP64 figure available)"}
+    # the plain FP64 GPU contraction on a few k-points, scaled
+    fp64 = None
+    if precision == "mixed" and a.fp64_k_sample > 0:
+        nk = min(a.fp64_k_sample, nkp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _lib.check(lib.pg_selfc_mwm(ptr(M), nk, P, N, ptr(W), nom, wkq, ptr(mwm_d), 0, nom, None, 0, ptr(status),
+                                    sh), "pg_selfc_mwm")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_m = e0.elapsed_time(e1) * 1e-3 * nkp / nk
+        fp64 = {"value": t_m + phase_ms["convolution"] * 1e-3, "unit": "s/q-point", "mwm_s": t_m,
+                "sample": f"FP64 contraction timed on {nk}/{nkp} k-points and scaled; convolution as measured"}
+    # end to end through the Python API: M from pinned host memory per k-chunk, Σc back to the host
+    e2e = None
+    if not a.no_e2e:
+        M_h = torch.empty((nkp, P, N), dtype=torch.complex128).pin_memory()
+        M_h.copy_(M)
+        sc_h = torch.empty((nkp, nb1, nom), dtype=torch.complex128).pin_memory()
+        ch = k_chunk if precision == "mixed" else max(1, min(nkp, int((4 << 30) // (16 * P * N))))
+
+        def e2e_step():
+            out = torch.empty((nkp, nom, P), dtype=torch.complex128, device="cuda")
+            for k0 in range(0, nkp, ch):
+                k1 = min(nkp, k0 + ch)
+                gsc.mwm(M_h[k0:k1], W, nb1, nb2, wkq, precision=precision, omega_batch=nb, out=out[k0:k1],
+                        work=workspace_mixed, status=status)
+            sc = gsc.convolution(out, ekq, om, wom, nb1, nb2)
+            sc_h.copy_(sc)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        et = time.perf_counter() - t0
+        e2e = {"value": et / a.steps, "unit": "s/q-point", "h2d_bytes_per_step": int(M_h.numel() * 16),
+               "d2h_bytes_per_step": int(sc_h.numel() * 16)}
+        del M_h
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        from oracle import selfc as osc
+        Mh = M[0].cpu().numpy().reshape(nb1, nb2, N)
+        Wh = W.cpu().numpy().transpose(2, 1, 0)                # (N, N, nom)
+        t0 = time.perf_counter()
+        mw = osc.mwm_k(Mh, Wh, wkq)
+        t_m = (time.perf_counter() - t0) * nkp
+        rows = 2
+        t0 = time.perf_counter()
+        osc.all_fr_convolutions(ekq[0], mw[:, :rows, :], om, wom)
+        t_c = (time.perf_counter() - t0) * nkp * nb1 / rows
+        cpu = {"value": t_m + t_c, "unit": "s/q-point", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"numpy mwm (pygw.py:3352-3356) on 1/{nkp} k-points, all {nom} frequencies, scaled: "
+                         f"{t_m:.1f}s; the restated convolution (fnc.f90:90-177, Python loops) on {rows}/{nb1} "
+                         f"bands of 1 k-point, scaled: {t_c:.1f}s"}
+    st = int(status.item())
+    sampler.stop()
+    clocks = sampler.window(wall0, wall1)
+    sampler.cleanup()
+    if rank == 0:
+        line = {"metric": "s/q-point for calc_selfc's mwm contraction + Matsubara convolution", "value": value,
+                "unit": "s/q-point", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+                "ms_per_step": dt / a.steps * 1e3, "higher_is_better": False, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "bf16-digits/f32-exact/f64",
+                "data": "synthetic",
+                "config": {"workload": workload_desc(w) + f"; selfc: nb1 {nb1} GW bands x nb2 {nb2} bands, "
+                                                          f"P {P}, {nkp} k-points, q {iq}",
+                           "precision": precision, "parallelism": "replicas", "k_chunk": k_chunk,
+                           "omega_batch": nb,
+                           "l2": "inputs larger than L2 (matrix elements %.1f GB read every step)"
+                                 % (M.numel() * 16 / 1e9)},
+                "roofline": roof, "kernel_status": st, "phases_ms": phase_ms, "fp64_gpu": fp64,
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks}
+        print(json.dumps(line), flush=True)
+
+
 # -------------------------------------------------------------------- main
 def main():
     a = parse()
@@ -505,6 +710,8 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from pygw_gb300 import _lib
 
+    if a.path == "selfc":
+        return run_selfc(a, w, rank, world, sampler)
     if w.npb_range or w.name == "C5":
         return run_batch_workload(a, w, rank, world, sampler)
     lib = _lib.load()

@@ -171,6 +171,47 @@ int pg_synth_minm(int nk, int k0, int iq, const double* enk, int nbnd, const int
                   int nb2, const int* kstart, const int* knb2, long long nrows, const double* sqv, int npb,
                   unsigned long long seed, void* out, void* stream);
 
+/* ---------------------------------------------- correlation self-energy
+ * Replaces the mwm loop of MatrixElements2Band.calc_selfc (pygw.py:3352-3364):
+ *   mwm[k][ω][p] = wkq · Σ_{I,J} conj(M[k][p][I]) · W[ω](I,J) · M[k][p][J]
+ * for the nk k-points of minm [nk][P][N] (P = nb1·nb2 band pairs, row-major
+ * p = ib1·nb2 + ib2) and the nom frequencies (or SVD functions) of
+ * W [nom][N][N] = ε⁻¹ − 1 as returned by pg_eps_inverse_* (column-major per
+ * frequency).  mixed = 0: FP64 (no workspace); mixed = 1: the split-precision
+ * tensor-core GEMM (five 8-bit digits per value, omega_batch frequencies per
+ * launch, workspace from the query).  d_status as for pg_chi0_mixed. */
+size_t pg_selfc_mwm_workspace(int nk, int P, int npb, int omega_batch, int mixed);
+int pg_selfc_mwm(const void* minm, int nk, int P, int npb, const void* eps, int nom, double wkq, void* mwm, int mixed,
+                 int omega_batch, void* work, size_t work_bytes, unsigned* d_status, void* stream);
+
+/* q = 0 terms of the same loop (pygw.py:3358-3363): for every row ie1 < nb1,
+ * mwm[k][ω][ie1, ie1 + off] += coefs2·head[ω] + coefs1·Σ_I M·epsw2[ω][I]
+ *                             + coefs1·Σ_I conj(M)·epsw1[ω][I],
+ * off = ibgw + ncg_c; head [nom], epsw1/epsw2 [nom][N] complex128. */
+int pg_selfc_mwm_q0(const void* minm, int nk, int nb1, int nb2, int npb, int off, int nom, const void* head,
+                    const void* epsw1, const void* epsw2, double coefs1, double coefs2, void* mwm, void* stream);
+
+/* Matsubara convolution of Compute_selfc_inside (mcommon.py:80-165):
+ * sc[k][ie1][iom] = Σ_ie2 fr_convolution2(enk[k][ie2], mwm[k][·][ie1,ie2], …)
+ * (all_fr_convolutions, fnc.f90:156-177) with enk [nk][nb2] the energies at
+ * k−q (core first).  n_dense > 0 selects the iopfreq 4 branch: mwm·(ω²+1) is
+ * interpolated to the dense mesh (omega_dense, womeg_dense) by the cubic-spline
+ * matrix spline [n_dense][nom] (row-major) and convolved there
+ * (few_fr_convolutions); womeg may then be null.  Workspace only for
+ * n_dense > 0. */
+size_t pg_selfc_convolution_workspace(int nk, int nb1, int nb2, int nom, int n_dense, int nl);
+int pg_selfc_convolution(const void* mwm, int nk, int nb1, int nb2, int nom, const double* enk, const double* omega,
+                         const double* womeg, int n_dense, const double* omega_dense, const double* womeg_dense,
+                         const double* spline, void* work, size_t work_bytes, void* sc, void* stream);
+
+/* SVD basis (mcommon.py:115-121): mwm [nk][nl][P] in the basis, Ul [nl][nom]
+ * complex128; sc[k][ie1][iom] = Σ_l Σ_ie2 mwm[k][l][ie1,ie2]·Cnl[k][l][ie2][iom]
+ * with Cnl from many_fr_convolutions (fnc.f90:139-154).  Workspace from
+ * pg_selfc_convolution_workspace(nk, nb1, nb2, nom, 0, nl). */
+int pg_selfc_convolution_svd(const void* mwm, int nk, int nb1, int nb2, int nl, int nom, const double* enk,
+                             const void* Ul, const double* omega, const double* womeg, void* work, size_t work_bytes,
+                             void* sc, void* stream);
+
 /* ------------------------------------------------------------ bookkeeping
  * Number of kernels this library has enqueued since it was loaded (all entry
  * points, all streams).  No counterpart in the reference. */

@@ -48,6 +48,16 @@ SIGNATURES = {
     "pg_chi0_mixed_layout": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
     "pg_wings_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_int, c_int, c_int, c_double,
                              c_void_p, c_void_p, c_void_p]),
+    "pg_selfc_mwm_workspace": (c_size_t, [c_int, c_int, c_int, c_int, c_int]),
+    "pg_selfc_mwm": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_double, c_void_p, c_int, c_int,
+                             c_void_p, c_size_t, c_void_p, c_void_p]),
+    "pg_selfc_mwm_q0": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                c_double, c_double, c_void_p, c_void_p]),
+    "pg_selfc_convolution_workspace": (c_size_t, [c_int] * 6),
+    "pg_selfc_convolution": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int,
+                                     c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_void_p]),
+    "pg_selfc_convolution_svd": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                         c_void_p, c_void_p, c_size_t, c_void_p, c_void_p]),
     "pg_launch_count": (ctypes.c_ulonglong, []),
     "pg_eps_inverse_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                                    c_void_p]),

@@ -28,6 +28,7 @@ SOURCES = {
     "chi0_mixed.cu": [],
     "eps_mixed.cu": [],
     "synth.cu": [],
+    "selfc.cu": [],
 }
 
 

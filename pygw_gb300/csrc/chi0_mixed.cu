@@ -72,6 +72,7 @@ struct OzParams {
   int gen;              // 0: upper block triangle of V·diag(w)·Vᵀ; 1: full A·Bᵀ
   int a_per_w;          // A planes per frequency (1) or shared by the batch (0)
   int nTb, nTbv, nCb;   // B: 128-row tiles, tiles with real rows, 256-row blocks
+  int nw;               // frequencies of this launch (≤ wb, the output's frequency stride)
 };
 
 // ------------------------------------------------------------ PTX helpers
@@ -252,25 +253,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int crank = (int)cluster_rank();
-  int rp, cb;
-  if (p.gen) {
-    rp = (blockIdx.x / CL) / p.nCb;
-    cb = (blockIdx.x / CL) % p.nCb;
-  } else {
-    tri_pair(blockIdx.x / CL, p.nC, rp, cb);
-  }
-  const int ti = 2 * rp + crank;                 // this CTA's 128-row tile
-  // column tiles 2cb, 2cb+1 of the block that are kept (upper triangle in the
-  // symmetric product) and hold real rows (at least one is computed, so both
-  // CTAs issue MMAs)
-  const int n_off = (!p.gen && ti > 2 * cb) ? 1 : 0;
-  int n_tiles = min(2 * cb + 2, p.nTbv) - (2 * cb + n_off);
-  if (n_tiles < 1) n_tiles = 1;
-  const int wl = blockIdx.y;        // frequency within the batch
-  const int split = blockIdx.z;
-  const int kb0 = split * p.kb_per_split;
-  const int kb1 = min(p.nkb, kb0 + p.kb_per_split);
   const uint16_t both = (uint16_t)((1u << CL) - 1u);
+  // Work units (output block, frequency, K split), numbered with the output
+  // block fastest; cluster cid takes units cid, cid + ncl, …  (the host launches
+  // one cluster per unit; a smaller grid makes the kernel persistent).
+  const int ncl = gridDim.x / CL, cid = blockIdx.x / CL;
+  const int nitems = p.gen ? p.nC * p.nCb : p.nC * (p.nC + 1) / 2;
+  const int nunits = nitems * p.nw * p.nsplit;
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < NST; i++) { mbar_init(full + i, 1); mbar_init(empty + i, CL); }
@@ -292,26 +281,49 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   cluster_sync_all();            // the peer's barriers exist before any multicast reaches them
   tc_fence_after();
   const uint32_t tmem = *tmem_base_slot;
-  const int nchunk_per_pass = (kb1 - kb0 + LBLK - 1) / LBLK;
+
+  // One unit: output block (rp, cb), this CTA's row tile ti, the kept column
+  // tiles (n_off, n_tiles), frequency wl and K range [kb0, kb1).
+  struct Unit { int rp, cb, ti, n_off, n_tiles, wl, split, kb0, kb1; };
+  auto unit = [&](int u) {
+    Unit U;
+    const int item = u % nitems, rest = u / nitems;
+    U.wl = rest % p.nw;
+    U.split = rest / p.nw;
+    if (p.gen) { U.rp = item / p.nCb; U.cb = item % p.nCb; }
+    else tri_pair(item, p.nC, U.rp, U.cb);
+    U.ti = 2 * U.rp + crank;
+    // column tiles 2cb, 2cb+1 that are kept (upper triangle of the symmetric
+    // product) and hold real rows (at least one, so both CTAs issue MMAs)
+    U.n_off = (!p.gen && U.ti > 2 * U.cb) ? 1 : 0;
+    U.n_tiles = min(2 * U.cb + 2, p.nTbv) - (2 * U.cb + U.n_off);
+    if (U.n_tiles < 1) U.n_tiles = 1;
+    U.kb0 = U.split * p.kb_per_split;
+    U.kb1 = min(p.nkb, U.kb0 + p.kb_per_split);
+    return U;
+  };
 
   if (warp == 0) {
     // ---------------------------------------------------------- TMA producer
-    // Load order: for d = 0..SD−1, s = 0..d (t = d − s), K-blocks kb0..kb1−1.
-    if (lane == 0 && kb1 > kb0) {
-      const int nkbs = kb1 - kb0;
-      const int total = (SD * (SD + 1) / 2) * nkbs;
+    // Per unit, load order: for d = 0..SD−1, s = 0..d (t = d − s), K-blocks kb0..kb1−1.
+    if (lane == 0) {
       int it = 0;
       bool ok = true;
-      for (; it < total && ok; it++) {
-        const int st = it % NST;
-        if (it >= NST) ok = mbar_wait(empty + st, ((it / NST) - 1) & 1, abort_flag, p.status);
-        if (!ok) break;
-        int ya, za, yb, zb;
-        load_coords<SD>(p, it, nkbs, kb0, ti, wl, cb, crank, ya, za, yb, zb);
-        unsigned char* sa = smem + st * STAGE_BYTES;
-        mbar_expect_tx(full + st, STAGE_BYTES);
-        tma_load_3d(sa, &tmA, full + st, 0, ya, za);
-        tma_load_3d_mc(sa + TILE_BYTES * (1 + crank), &tmB, full + st, 0, yb, zb, both);
+      for (int u = cid; u < nunits && ok; u += ncl) {
+        const Unit U = unit(u);
+        const int nkbs = U.kb1 - U.kb0;
+        const int total = (SD * (SD + 1) / 2) * nkbs;
+        for (int i = 0; i < total && ok; i++, it++) {
+          const int st = it % NST;
+          if (it >= NST) ok = mbar_wait(empty + st, ((it / NST) - 1) & 1, abort_flag, p.status);
+          if (!ok) break;
+          int ya, za, yb, zb;
+          load_coords<SD>(p, i, nkbs, U.kb0, U.ti, U.wl, U.cb, crank, ya, za, yb, zb);
+          unsigned char* sa = smem + st * STAGE_BYTES;
+          mbar_expect_tx(full + st, STAGE_BYTES);
+          tma_load_3d(sa, &tmA, full + st, 0, ya, za);
+          tma_load_3d_mc(sa + TILE_BYTES * (1 + crank), &tmB, full + st, 0, yb, zb, both);
+        }
       }
       // drain: the last phase of every stage must have been read by both CTAs'
       // MMAs (so every load and every remote arrival on this CTA has landed)
@@ -324,39 +336,44 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
   } else if (warp == 1) {
     // ---------------------------------------------------------- MMA issuer
-    if (lane == 0 && kb1 > kb0) {
-      const uint32_t idesc = idesc_m128(TM * n_tiles);
-      int it = 0, c = 0;
+    if (lane == 0) {
+      int it = 0, c = 0, G = 0;          // loads, chunks and digit groups consumed so far
       bool ok = true;
-      for (int d = 0; d < SD && ok; d++) {
-        if (d > 0) ok = mbar_wait(group_done, (d - 1) & 1, abort_flag, p.status);
-        if (!ok) break;
-        bool used[2] = {false, false};
-        for (int s = 0; s <= d && ok; s++) {
-          for (int ch = 0; ch < nchunk_per_pass && ok; ch++, c++) {
-            const int b = c & 1;
-            if (c >= 2) ok = mbar_wait(acc_empty + b, ((c >> 1) - 1) & 1, abort_flag, p.status);
-            if (!ok) break;
-            tc_fence_after();
-            const uint32_t dcol = tmem + (uint32_t)(b * TN + n_off * TM);
-            const int cb0 = kb0 + ch * LBLK, cb1 = min(kb1, cb0 + LBLK);
-            for (int kb = cb0; kb < cb1; kb++, it++) {
-              const int st = it % NST;
-              ok = mbar_wait(full + st, (it / NST) & 1, abort_flag, p.status);
+      for (int u = cid; u < nunits && ok; u += ncl) {
+        const Unit U = unit(u);
+        const uint32_t idesc = idesc_m128(TM * U.n_tiles);
+        const int nchunk_per_pass = (U.kb1 - U.kb0 + LBLK - 1) / LBLK;
+        for (int d = 0; d < SD && ok; d++, G++) {
+          // the epilogue has combined the previous group (its remainders are read)
+          if (G > 0) ok = mbar_wait(group_done, (G - 1) & 1, abort_flag, p.status);
+          if (!ok) break;
+          bool used[2] = {false, false};
+          for (int s = 0; s <= d && ok; s++) {
+            for (int ch = 0; ch < nchunk_per_pass && ok; ch++, c++) {
+              const int b = c & 1;
+              if (c >= 2) ok = mbar_wait(acc_empty + b, ((c >> 1) - 1) & 1, abort_flag, p.status);
               if (!ok) break;
               tc_fence_after();
-              const uint32_t sa = smem_u32(smem + st * STAGE_BYTES);
-              const uint64_t ad = sdesc_sw128(sa), bd = sdesc_sw128(sa + TILE_BYTES * (1 + n_off));
+              const uint32_t dcol = tmem + (uint32_t)(b * TN + U.n_off * TM);
+              const int cb0 = U.kb0 + ch * LBLK, cb1 = min(U.kb1, cb0 + LBLK);
+              for (int kb = cb0; kb < cb1; kb++, it++) {
+                const int st = it % NST;
+                ok = mbar_wait(full + st, (it / NST) & 1, abort_flag, p.status);
+                if (!ok) break;
+                tc_fence_after();
+                const uint32_t sa = smem_u32(smem + st * STAGE_BYTES);
+                const uint64_t ad = sdesc_sw128(sa), bd = sdesc_sw128(sa + TILE_BYTES * (1 + U.n_off));
 #pragma unroll
-              for (int k = 0; k < KB / 16; k++) {
-                const uint32_t accumulate = (used[b] || kb > cb0 || k > 0) ? 1u : 0u;
-                tc_mma(dcol, ad + (uint64_t)(2 * k), bd + (uint64_t)(2 * k), idesc, accumulate);
+                for (int k = 0; k < KB / 16; k++) {
+                  const uint32_t accumulate = (used[b] || kb > cb0 || k > 0) ? 1u : 0u;
+                  tc_mma(dcol, ad + (uint64_t)(2 * k), bd + (uint64_t)(2 * k), idesc, accumulate);
+                }
+                tc_commit_mc(empty + st, both);   // stage free in both CTAs once these MMAs have read it
               }
-              tc_commit_mc(empty + st, both);   // stage free in both CTAs once these MMAs have read it
+              if (!ok) break;
+              used[b] = true;
+              tc_commit(acc_full + b);     // chunk complete
             }
-            if (!ok) break;
-            used[b] = true;
-            tc_commit(acc_full + b);     // chunk complete
           }
         }
       }
@@ -370,71 +387,75 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int q = warp & 3;                        // TMEM lane quarter this warp may access
     const int h = (warp - 2) >> 2;                 // column half of the block
     const int row = q * 32 + lane;                 // accumulator row (A tile row)
-    const int tj = 2 * cb + h;
-    const bool active = h >= n_off && h < n_off + n_tiles;
-    const bool stored = p.gen || tj >= ti;         // tile (ti, tj) is kept
     const uint32_t t_b0 = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * TM);
     const uint32_t t_b1 = t_b0 + TN;
-    const int pair = p.gen ? ti * p.nTb + tj : stored ? ti * p.nT - ti * (ti - 1) / 2 + (tj - ti) : 0;
-    double* out = p.out + ((((size_t)split * p.wb + wl) * p.npair + pair) * TM) * TM;
     float hi[TM];                                  // high accumulator: multiples of 2^12, exact below 2^36
     int c = 0;
-    bool ok = kb1 > kb0;
-    for (int d = 0; d < SD && ok; d++) {
+    bool ok = true;
+    for (int u = cid; u < nunits && ok; u += ncl) {
+      const Unit U = unit(u);
+      const int tj = 2 * U.cb + h;
+      const bool active = h >= U.n_off && h < U.n_off + U.n_tiles;
+      const bool stored = p.gen || tj >= U.ti;     // tile (ti, tj) is kept
+      const int pair = p.gen ? U.ti * p.nTb + tj : stored ? U.ti * p.nT - U.ti * (U.ti - 1) / 2 + (tj - U.ti) : 0;
+      double* out = p.out + ((((size_t)U.split * p.wb + U.wl) * p.npair + pair) * TM) * TM;
+      const int nchunk_per_pass = (U.kb1 - U.kb0 + LBLK - 1) / LBLK;
+      for (int d = 0; d < SD && ok; d++) {
 #pragma unroll
-      for (int i = 0; i < TM; i++) hi[i] = 0.0f;
-      const int nchunks_group = (d + 1) * nchunk_per_pass;
-      const int c_first = c;
-      for (int gc = 0; gc < nchunks_group && ok; gc++, c++) {
-        const int b = c & 1;
-        ok = mbar_wait(acc_full + b, (c >> 1) & 1, abort_flag, p.status);
-        if (!ok) break;
-        tc_fence_after();
-        if (active) {
-          const uint32_t tl = b ? t_b1 : t_b0;
+        for (int i = 0; i < TM; i++) hi[i] = 0.0f;
+        const int nchunks_group = (d + 1) * nchunk_per_pass;
+        const int c_first = c;
+        for (int gc = 0; gc < nchunks_group && ok; gc++, c++) {
+          const int b = c & 1;
+          ok = mbar_wait(acc_full + b, (c >> 1) & 1, abort_flag, p.status);
+          if (!ok) break;
+          tc_fence_after();
+          if (active) {
+            const uint32_t tl = b ? t_b1 : t_b0;
 #pragma unroll
-          for (int cc = 0; cc < TM / 16; cc++) {
-            float lo[16];
-            tmem_ld16(tl + cc * 16, lo);
+            for (int cc = 0; cc < TM / 16; cc++) {
+              float lo[16];
+              tmem_ld16(tl + cc * 16, lo);
 #pragma unroll
-            for (int i = 0; i < 16; i++) {
-              const float hh = rintf(lo[i] * (1.0f / 4096.0f)) * 4096.0f;   // multiple of 2^12
-              lo[i] = lo[i] - hh;                                            // |residual| ≤ 2^11
-              hi[cc * 16 + i] += hh;
-            }
-            tmem_st16(tl + cc * 16, lo);
-          }
-        }
-        if (gc == nchunks_group - 1 && active) {
-          // group complete: I_d = high + both low remainders (|r| ≤ 2^11, so r0 + r1 is
-          // exact in FP32 and high + r0 + r1 exact in FP64), scaled by 2^(−8d);
-          // 8 columns at a time keep the live registers to hi[] + 16
-          const bool used0 = nchunks_group >= 2 || (c_first & 1) == 0;
-          const bool used1 = nchunks_group >= 2 || (c_first & 1) == 1;
-          const double scale = ldexp(1.0, -8 * d);
-#pragma unroll
-          for (int cc = 0; cc < TM / 8; cc++) {
-            float l0[8], l1[8];
-            if (used0) tmem_ld8(t_b0 + cc * 8, l0);
-            if (used1) tmem_ld8(t_b1 + cc * 8, l1);
-#pragma unroll
-            for (int i = 0; i < 8; i++) {
-              const float r = (used0 ? l0[i] : 0.0f) + (used1 ? l1[i] : 0.0f);
-              const double v = (double)hi[cc * 8 + i] + (double)r;
-              double& o = out[(size_t)(cc * 8 + i) * TM + row];
-              o = (d == 0) ? v * scale : o + v * scale;
+              for (int i = 0; i < 16; i++) {
+                const float hh = rintf(lo[i] * (1.0f / 4096.0f)) * 4096.0f;   // multiple of 2^12
+                lo[i] = lo[i] - hh;                                            // |residual| ≤ 2^11
+                hi[cc * 16 + i] += hh;
+              }
+              tmem_st16(tl + cc * 16, lo);
             }
           }
+          if (gc == nchunks_group - 1 && active) {
+            // group complete: I_d = high + both low remainders (|r| ≤ 2^11, so r0 + r1 is
+            // exact in FP32 and high + r0 + r1 exact in FP64), scaled by 2^(−8d);
+            // 8 columns at a time keep the live registers to hi[] + 16
+            const bool used0 = nchunks_group >= 2 || (c_first & 1) == 0;
+            const bool used1 = nchunks_group >= 2 || (c_first & 1) == 1;
+            const double scale = ldexp(1.0, -8 * d);
+#pragma unroll
+            for (int cc = 0; cc < TM / 8; cc++) {
+              float l0[8], l1[8];
+              if (used0) tmem_ld8(t_b0 + cc * 8, l0);
+              if (used1) tmem_ld8(t_b1 + cc * 8, l1);
+#pragma unroll
+              for (int i = 0; i < 8; i++) {
+                const float r = (used0 ? l0[i] : 0.0f) + (used1 ? l1[i] : 0.0f);
+                const double v = (double)hi[cc * 8 + i] + (double)r;
+                double& o = out[(size_t)(cc * 8 + i) * TM + row];
+                o = (d == 0) ? v * scale : o + v * scale;
+              }
+            }
+          }
+          tc_fence_before();
+          mbar_arrive(acc_empty + b);
+          if (gc == nchunks_group - 1) mbar_arrive(group_done);
         }
-        tc_fence_before();
-        mbar_arrive(acc_empty + b);
-        if (gc == nchunks_group - 1) mbar_arrive(group_done);
       }
-    }
-    if (stored && (!active || kb1 <= kb0)) {
-      for (int i = 0; i < TM; i++) out[(size_t)i * TM + row] = 0.0;        // padding tile or empty K-split
-    } else if (stored && !ok) {
-      for (int i = 0; i < TM; i++) out[(size_t)i * TM + row] = __longlong_as_double(0x7ff8dead00000000LL);
+      if (stored && !active) {
+        for (int i = 0; i < TM; i++) out[(size_t)i * TM + row] = 0.0;        // padding tile
+      } else if (stored && !ok) {
+        for (int i = 0; i < TM; i++) out[(size_t)i * TM + row] = __longlong_as_double(0x7ff8dead00000000LL);
+      }
     }
   }
   tc_fence_before();
@@ -707,6 +728,7 @@ struct MixedLayout {
 static size_t gemm_smem_bytes() { return (size_t)NST * STAGE_BYTES + 1024 + 256; }
 
 // CTAs of k_ozaki_gemm that run at once on the current device (cached per device).
+#include <algorithm>
 #include <mutex>
 static std::mutex g_cap_mutex;
 static int g_cap[64] = {0};
@@ -885,7 +907,12 @@ static int chi0_mixed_impl(const void* minm, int nkp, int k0, const int* kstart,
     k_digits_B<<<dim3((unsigned)((L.K_pad + 1023) / 1024), L.R_pad), 256, 0, s>>>(adig, eA, wpair, fB, L.R, L.R_pad,
                                                                                   L.K_pad, nw, bdig);
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(CL * L.nitems), (unsigned)nw, (unsigned)L.nsplit);
+    op.nw = nw;
+    // one cluster per unit: the hardware schedules the units in waves, whose
+    // staggered starts spread the digit traffic over time (a grid of
+    // co-resident clusters looping over the units measured 12 % slower at C3)
+    const int nunits = L.nitems * nw * L.nsplit;
+    cfg.gridDim = dim3((unsigned)(CL * nunits), 1, 1);
     cfg.blockDim = dim3(NTHREADS);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
@@ -927,14 +954,14 @@ extern "C" int pg_chi0_mixed_accumulate(const void* minm, int nk_chunk, int k0, 
 }
 
 // Full product for the refinement of ε⁻¹ (see ozaki.h).
-int pgm::launch_gemm_general(const __nv_bfloat16* adig, const __nv_bfloat16* bdig, int sd, int R_padA, int R_padB,
-                             int nTbv, int nkb, int nw, double* out, unsigned* status, cudaStream_t s) {
+int pgm::launch_gemm_general(const __nv_bfloat16* adig, const __nv_bfloat16* bdig, int sd, int a_per_w, int R_padA,
+                             int R_padB, int nTbv, int nkb, int nw, double* out, unsigned* status, cudaStream_t s) {
   // group sums stay below 2^35: sd pairs · nkb·64 · 129² < 2^35
   if (R_padA <= 0 || R_padB <= 0 || R_padA % TN || R_padB % TN || nkb <= 0 || nw <= 0 || (sd != 5 && sd != 6) ||
       (long long)sd * nkb * 64 * 16641 >= (1ll << 35))
     return PG_EARG;
   CUtensorMap mapA, mapB;
-  if (!make_map(&mapA, (void*)adig, R_padA, (long long)nw * sd * nkb)) return PG_ECUDA;
+  if (!make_map(&mapA, (void*)adig, R_padA, (long long)(a_per_w ? nw : 1) * sd * nkb)) return PG_ECUDA;
   if (!make_map(&mapB, (void*)bdig, R_padB, (long long)nw * sd * nkb)) return PG_ECUDA;
   const size_t smem = gemm_smem_bytes();
   auto kern = (sd == 6) ? k_ozaki_gemm<6> : k_ozaki_gemm<5>;
@@ -944,7 +971,7 @@ int pgm::launch_gemm_general(const __nv_bfloat16* adig, const __nv_bfloat16* bdi
   memset(&op, 0, sizeof(op));
   op.out = out; op.status = status;
   op.R_pad = R_padA; op.nT = R_padA / TM; op.nTv = R_padA / TM; op.nC = R_padA / TN;
-  op.gen = 1; op.a_per_w = 1; op.nTb = R_padB / TM; op.nTbv = nTbv; op.nCb = R_padB / TN;
+  op.gen = 1; op.a_per_w = a_per_w ? 1 : 0; op.nTb = R_padB / TM; op.nTbv = nTbv; op.nCb = R_padB / TN;
   op.npair = op.nT * op.nTb; op.nkb = nkb; op.kb_per_split = nkb; op.nsplit = 1; op.wb = nw;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -952,7 +979,8 @@ int pgm::launch_gemm_general(const __nv_bfloat16* adig, const __nv_bfloat16* bdi
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)(CL * op.nC * op.nCb), (unsigned)nw, 1);
+  op.nw = nw;
+  cfg.gridDim = dim3((unsigned)(CL * op.nC * op.nCb * nw), 1, 1);
   cfg.blockDim = dim3(NTHREADS);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;

@@ -226,11 +226,12 @@ __global__ void k_col_exp(const T* M, int N, int R_pad, int two_rows, int* e) {
   }
 }
 
-// S signed 8-bit digits of x relative to 2^e (exact FP64 arithmetic).
-__device__ __forceinline__ void digitsS(double x, int e, __nv_bfloat16 (&d)[S]) {
+// ND signed 8-bit digits of x relative to 2^e (exact FP64 arithmetic).
+template <int ND>
+__device__ __forceinline__ void digitsS(double x, int e, __nv_bfloat16 (&d)[ND]) {
   double y = ldexp(x, -e);
 #pragma unroll
-  for (int s = 0; s < S; s++) {
+  for (int s = 0; s < ND; s++) {
     const double t = y * 256.0;
     const double dg = rint(t);
     y = t - dg;
@@ -248,8 +249,8 @@ __global__ void k_digits_herm(const double2* __restrict__ A, int N, int R_pad, i
   const double2 x = A[(size_t)N * N * w + (size_t)N * r + k];   // A(k, r) = conj A(r, k)
   const int e = eA[(size_t)R_pad * w + r];
   __nv_bfloat16 dre[S], dim[S];
-  digitsS(x.x, e, dre);
-  digitsS(x.y, e, dim);
+  digitsS<S>(x.x, e, dre);
+  digitsS<S>(x.y, e, dim);
 #pragma unroll
   for (int s = 0; s < S; s++) {
     const int pl = w * S + s;
@@ -261,19 +262,19 @@ __global__ void k_digits_herm(const double2* __restrict__ A, int N, int R_pad, i
 }
 
 // B digits: row j = [Re X(:, j); Im X(:, j)].  Grid (ceil(N/256), N, nw).
-template <typename T>
+template <typename T, int ND>
 __global__ void k_digits_cols(const T* __restrict__ X, int N, int R_pad, int nkb, const int* fB, __nv_bfloat16* bdig) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y, w = blockIdx.z;
   if (k >= N) return;
   const double2 x = ld2(X + (size_t)N * N * w + (size_t)N * j + k);
   const int e = fB[(size_t)R_pad * w + j];
-  __nv_bfloat16 dre[S], dim[S];
-  digitsS(x.x, e, dre);
-  digitsS(x.y, e, dim);
+  __nv_bfloat16 dre[ND], dim[ND];
+  digitsS<ND>(x.x, e, dre);
+  digitsS<ND>(x.y, e, dim);
 #pragma unroll
-  for (int s = 0; s < S; s++) {
-    const int pl = w * S + s;
+  for (int s = 0; s < ND; s++) {
+    const int pl = w * ND + s;
     bdig[digit_index(pl, j, k, R_pad, nkb)] = dre[s];
     bdig[digit_index(pl, j, N + k, R_pad, nkb)] = dim[s];
   }
@@ -403,10 +404,10 @@ static int refine_step(const T* X, double2* dst, const Layout& L, char* w, int n
   if (cudaMemsetAsync(fB, 0, sizeof(int) * (size_t)L.R_padB * nw, s) != cudaSuccess) return PG_ECUDA;
   if (cudaMemsetAsync(bdig, 0, (size_t)2 * S * L.R_padB * L.K_pad * nw, s) != cudaSuccess) return PG_ECUDA;
   k_col_exp<T><<<dim3(N, nw), 256, 0, s>>>(X, N, L.R_padB, 0, fB);
-  k_digits_cols<T><<<dim3((N + 255) / 256, N, nw), 256, 0, s>>>(X, N, L.R_padB, L.nkb, fB, bdig);
+  k_digits_cols<T, S><<<dim3((N + 255) / 256, N, nw), 256, 0, s>>>(X, N, L.R_padB, L.nkb, fB, bdig);
   pg_count_launches(2);
   double* out = (double*)(w + L.out);
-  const int rc = pgm::launch_gemm_general((const __nv_bfloat16*)(w + L.adig), bdig, S, L.R_padA, L.R_padB,
+  const int rc = pgm::launch_gemm_general((const __nv_bfloat16*)(w + L.adig), bdig, S, 1, L.R_padA, L.R_padB,
                                           (N + pgm::OZ_TILE - 1) / pgm::OZ_TILE, L.nkb, nw, out, status, s);
   if (rc != PG_OK) return rc;
   double2* R = (double2*)(w + L.res);
@@ -415,6 +416,22 @@ static int refine_step(const T* X, double2* dst, const Layout& L, char* w, int n
   k_correct<T><<<dim3((N + 63) / 64, (N + 63) / 64, nw), 256, 0, s>>>(X, R, N, dst);
   pg_count_launches(2);
   return PG_OK;
+}
+
+// Exponents and nd (5 or 6) digits of the columns of X[nw][N][N] complex128
+// as B rows [Re X(:,j); Im X(:,j)] (bdig and fB zeroed first).
+int launch_cols_digits(const double2* X, int N, int nw, int R_pad, int nkb, int nd, int* fB, __nv_bfloat16* bdig,
+                       cudaStream_t s) {
+  if (nd != 5 && nd != 6) return PG_EARG;
+  if (cudaMemsetAsync(fB, 0, sizeof(int) * (size_t)R_pad * nw, s) != cudaSuccess) return PG_ECUDA;
+  if (cudaMemsetAsync(bdig, 0, (size_t)2 * nd * R_pad * nkb * 64 * nw, s) != cudaSuccess) return PG_ECUDA;
+  k_col_exp<double2><<<dim3(N, nw), 256, 0, s>>>(X, N, R_pad, 0, fB);
+  if (nd == 5)
+    k_digits_cols<double2, 5><<<dim3((N + 255) / 256, N, nw), 256, 0, s>>>(X, N, R_pad, nkb, fB, bdig);
+  else
+    k_digits_cols<double2, 6><<<dim3((N + 255) / 256, N, nw), 256, 0, s>>>(X, N, R_pad, nkb, fB, bdig);
+  pg_count_launches(2);
+  return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ECUDA;
 }
 
 }  // namespace pgx

@@ -40,7 +40,17 @@ __device__ __forceinline__ int row_exponent(float bound) {
 // ≈ 2^-40 to ≈ 2^-48 of the row scales).
 // out: [nw][R_padA/128 · R_padB/128 tiles][128 (col)][128 (row)] FP64.
 // nTbv: B tiles holding real rows.  Returns a PG_* code.
-int launch_gemm_general(const __nv_bfloat16* adig, const __nv_bfloat16* bdig, int sd, int R_padA, int R_padB,
-                        int nTbv, int nkb, int nw, double* out, unsigned* status, cudaStream_t s);
+// a_per_w: A digits per frequency (1) or one set shared by the frequencies (0).
+int launch_gemm_general(const __nv_bfloat16* adig, const __nv_bfloat16* bdig, int sd, int a_per_w, int R_padA,
+                        int R_padB, int nTbv, int nkb, int nw, double* out, unsigned* status, cudaStream_t s);
+
+}  // namespace pgm
+
+namespace pgx {
+// Exponents and nd (5 or 6) digits of the columns of X[nw][N][N] (complex128,
+// column-major per frequency) as B rows [Re X(:,j); Im X(:,j)] of the general
+// product; bdig/fB are laid out for R_pad rows and nkb K-blocks.
+int launch_cols_digits(const double2* X, int N, int nw, int R_pad, int nkb, int nd, int* fB, __nv_bfloat16* bdig,
+                       cudaStream_t s);
 
 }  // namespace pgm

@@ -358,17 +358,20 @@ def chi0_eps(kcw, minm, nkp, npb, nb1, nb2, nom, pm_k=None, head=None, k_chunk=N
 
 
 class MatrixElements2Band:
-    """Stand-in for the reference class with the GB300 ``calc_eps``.
+    """Stand-in for the reference class with the GB300 ``calc_eps`` and ``calc_selfc``.
 
     ``calc_minm(ik, iq, band_limits, mode, ...)`` must return
-    ``(minm0, minc0)`` as in the reference (pygw.py:3096-3098); the synthetic
-    generator provides one (``synthetic_matrix_elements``).
+    ``(minm0, minc0)`` as in the reference (pygw.py:3096-3098 for
+    'polarization', 3342-3349 for 'selfe'); the synthetic generator provides
+    one (``synthetic_matrix_elements``).  singc1/singc2 are the q→0
+    singularity coefficients calc_selfc uses at q = 0 (pygw.py:3310-3311).
     """
 
-    def __init__(self, calc_minm, matsize, pm_k=None):
+    def __init__(self, calc_minm, matsize, pm_k=None, singc1=0.0, singc2=0.0):
         self.calc_minm = calc_minm
         self.matsize = matsize
         self.pm_k = pm_k
+        self.singc1, self.singc2 = singc1, singc2
 
     def calc_eps(self, iq, head_quantities, strc, in1, latgen, kqm, ks, radf, pw, pb, core, kw, fr, kcw, ddir, dUl,
                  Ul, fout):
@@ -393,3 +396,10 @@ class MatrixElements2Band:
             for iom in range(eps.shape[2]):
                 print("Tr(1/eps[%3d]-1) = %18.14f" % (iom + 1, np.trace(eps[:, :, iom]).real), file=fout)
         return eps, epsw1, epsw2, head_out
+
+    def calc_selfc(self, iq, eps, epsw1, epsw2, head, strc, in1, latgen, kqm, ks, radf, pw, pb, core, kw, fr, ddir,
+                   dUl, Ul, fout, PRINT=True):
+        """pygw.py:3299 — Σc contributions sc_p[nirkp, nbgw − ibgw, nom] of this q (see selfc.calc_selfc)."""
+        from .selfc import calc_selfc
+        return calc_selfc(self, iq, eps, epsw1, epsw2, head, strc, in1, latgen, kqm, ks, radf, pw, pb, core, kw, fr,
+                          ddir, dUl, Ul, fout, PRINT=PRINT)
