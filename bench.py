@@ -277,6 +277,26 @@ def mixed_tile_area(npb):
     return area
 
 
+def bf16_peak():
+    """The bf16 denominator for a kernel timed inside a multi-second step: the
+    measured sustained figure (the burst one is for a kernel timed alone)."""
+    peaks = json.load(open(PEAKS_FILE)) if os.path.exists(PEAKS_FILE) else {}
+    if "bf16_tflops_sustained" in peaks:
+        return peaks["bf16_tflops_sustained"], "of measured (sustained)"
+    if "bf16_tflops" in peaks:
+        return peaks["bf16_tflops"], "of measured (burst)"
+    return 1700.0, "of fallback (sustained)"
+
+
+# DRAM bytes (read + written) of one k_ozaki_gemm launch of the χ0 digit GEMM,
+# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one capture)
+# per launch shape: (workload, N_PB, k-points, frequencies per launch).
+MEASURED_GEMM_TRAFFIC = {
+    ("C3", 1200, 216, 1): 423.06e9 + 0.64e9,
+    ("C3", 1200, 216, 2): 1050.0e9 + 1.83e9,
+}
+
+
 # GB300's FP64 rate (CUDA cores; it has no faster FP64 tensor path).  The
 # measured peaks file holds HBM and bf16 figures only, so the FP64 roofline
 # of the plain path is quoted against this nominal figure.
@@ -399,13 +419,12 @@ def run_batch_workload(a, w, rank, world, sampler):
     value = dt / (a.steps * nq)
     nb1, nb2, nkp, nom = bt.nb1, bt.nb2, bt.nkp, bt.nom
     alg = sum(8.0 * t.npb * t.npb * k * nom for t, k in zip(tasks, bt.ktot))   # ragged K = Σ_k nb1·knb2[k]
-    peaks = json.load(open(PEAKS_FILE)) if os.path.exists(PEAKS_FILE) else {}
-    peak = peaks.get("bf16_tflops", 1900.0)
+    peak, peak_note = bf16_peak()
     roof = {"kernel": "whole step (weights + split-precision chi0 + mixed eps^-1, one graph)", "bound": "tensor",
             "achieved": alg / (dt / a.steps) / 1e12, "peak": peak, "unit": "TFLOP/s",
             "frac": alg / (dt / a.steps) / 1e12 / peak, "traffic": None,
             "note": "algorithmic 8*N_q^2*K_q*Nw summed over q (K_q = ragged window total) / step time; "
-                    "the per-kernel roofline of k_ozaki_gemm is in the C3 line"}
+                    "the per-kernel roofline of k_ozaki_gemm is in the C3 line; peak = bf16 " + peak_note}
     # plain FP64 GPU path, one q at a time on the full window: weights and inverse timed in full,
     # the FP64 contraction on a few k-points (device-generated M) and scaled
     fp64 = None
@@ -586,10 +605,8 @@ def run_selfc(a, w, rank, world, sampler):
     # roofline of the contraction: the reference's complex GEMM count 8·P·N²·nω per k-point
     mw_s = sum(e0.elapsed_time(e1) for e0, e1, _ in g_ev) * 1e-3
     alg = sum(8.0 * nk * P * N * N * nom for _, _, nk in g_ev)
-    peaks = json.load(open(PEAKS_FILE)) if os.path.exists(PEAKS_FILE) else {}
     if precision == "mixed":
-        peak = peaks.get("bf16_tflops", 1900.0)
-        note = "of measured" if "bf16_tflops" in peaks else "of fallback"
+        peak, note = bf16_peak()
         rpad_b = -(-N // 256) * 256
         kpad = -(-2 * N // 64) * 64
         exe = sum(15 * 2.0 * (-(-2 * nk * P // 256) * 256) * min(rpad_b, -(-N // 128) * 128) * kpad * nom
@@ -762,9 +779,7 @@ def main():
     for st in inp.statuses:
         status_bits |= int(st.item())
     if a.precision == "mixed":
-        peaks = json.load(open(PEAKS_FILE)) if os.path.exists(PEAKS_FILE) else {}
-        peak = peaks.get("bf16_tflops", 1900.0)
-        peak_note = "of measured" if "bf16_tflops" in peaks else "of fallback"
+        peak, peak_note = bf16_peak()
         kpad = ((inp.nkp * nb1 * nb2 + 63) // 64) * 64
         # per launch: one batch of wb frequencies (the last batch may be smaller)
         g_ms = [s_.elapsed_time(e_) for s_, e_ in inp.gemm_timers]
@@ -773,15 +788,25 @@ def main():
         alg = sum(8.0 * npb * npb * nb1 * nb2 * inp.nkp * nw for nw in nws)
         exe = sum(15 * 2.0 * mixed_tile_area(npb) * kpad * nw for nw in nws)
         g_s = sum(g_ms) * 1e-3
+        # distinct digit bytes of one launch: the A planes once, the B planes of each frequency
+        rpad = -(-2 * npb // 256) * 256
+        dig_bytes = 5 * rpad * kpad * 2 * (1 + inp.wb)
+        traffic = MEASURED_GEMM_TRAFFIC.get((w.name, npb, inp.nkp, inp.wb))
+        hbm = json.load(open(PEAKS_FILE)).get("hbm_gbs") if os.path.exists(PEAKS_FILE) else None
         roof = {"kernel": "k_ozaki_gemm", "bound": "tensor", "achieved": alg / g_s / 1e12,
-                "peak": peak, "unit": "TFLOP/s", "frac": alg / g_s / 1e12 / peak, "traffic": None,
+                "peak": peak, "unit": "TFLOP/s", "frac": alg / g_s / 1e12 / peak, "traffic": traffic,
+                "algorithmic_bytes": dig_bytes,
+                "dram_frac": (traffic / (g_s / len(g_ms)) / 1e9 / hbm) if traffic and hbm else None,
                 "launches": len(g_ms), "ms_per_launch": sum(g_ms) / max(1, len(g_ms)),
                 "executed_bf16_tflops": exe / g_s / 1e12,
                 "executed_frac": exe / g_s / 1e12 / peak,
                 "chi0_phase_algorithmic_tflops": achieved,
                 "note": "achieved = 8*N_PB^2*P*Nk*Nw per launch (the reference's complex FP64 GEMM count) / "
                         "CUDA-event launch time of k_ozaki_gemm; executed_bf16 = 15 digit-pair bf16 products "
-                        "over the computed 128x256 / 128x128 tiles; peak = bf16 " + peak_note}
+                        "over the computed 128x256 / 128x128 tiles; peak = bf16 " + peak_note + "; traffic = "
+                        "DRAM bytes per launch from one ncu capture of this launch shape (null if not captured), "
+                        "algorithmic_bytes = the distinct digit planes the launch reads, dram_frac = traffic / "
+                        "launch time / measured HBM copy bandwidth"}
     else:
         peak = FP64_NOMINAL_TFLOPS
         roof = {"kernel": "k_chi0_f64", "bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",

@@ -193,7 +193,7 @@ class Batch:
         out = []
         for kc in kcs:
             wfit = self._fit_omega_batch(npb, kc)
-            for wb in sorted({wfit, max(1, wfit // 2)}, reverse=True):
+            for wb in sorted({wfit, max(1, wfit // 2), 1}, reverse=True):
                 out.append((kc, wb))
         return out
 
