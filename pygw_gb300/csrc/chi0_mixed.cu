@@ -73,6 +73,7 @@ struct OzParams {
   int a_per_w;          // A planes per frequency (1) or shared by the batch (0)
   int nTb, nTbv, nCb;   // B: 128-row tiles, tiles with real rows, 256-row blocks
   int nw;               // frequencies of this launch (≤ wb, the output's frequency stride)
+  int wl0;              // B planes of this launch start at frequency wl0 of the digit array
 };
 
 // ------------------------------------------------------------ PTX helpers
@@ -231,7 +232,7 @@ __device__ __forceinline__ void load_coords(const OzParams& p, int i, int nkbs, 
   ya = ti * TM;
   za = ((p.a_per_w ? wl * SD : 0) + s_) * p.nkb + kb;
   yb = cb * TN + crank * TM;
-  zb = (wl * SD + t_) * p.nkb + kb;
+  zb = ((p.wl0 + wl) * SD + t_) * p.nkb + kb;
 }
 
 // ------------------------------------------------------ the digit GEMM
@@ -666,13 +667,16 @@ __global__ void k_digits_B(const __nv_bfloat16* __restrict__ adig, const int* eA
     const float4 w01 = wp[0], w23 = wp[1];
     const float wh[4] = {w01.x, w01.z, w23.x, w23.z}, wo[4] = {w01.y, w01.w, w23.y, w23.w};
     const int sh = (r < R) ? (eA[r] - fB[(size_t)wl * R_pad + r]) : 0;
+    // 2^sh as a float when it is a normal number (a multiply then scales exactly as ldexpf does)
+    const bool fast = sh >= -126 && sh <= 127;
+    const float p2 = fast ? __int_as_float((sh + 127) << 23) : 1.0f;
     float dg[S][4];
 #pragma unroll
     for (int j = 0; j < 4; j++) {
       const float ph = vhi[j] * wh[j];
       const float pe = fmaf(vhi[j], wh[j], -ph);
       const float pl = pe + (vhi[j] * wo[j] + vlo[j] * wh[j]);
-      float yh = ldexpf(ph, sh), yl = ldexpf(pl, sh);
+      float yh = fast ? ph * p2 : ldexpf(ph, sh), yl = fast ? pl * p2 : ldexpf(pl, sh);
       two_sum(yh, yl, yh, yl);
 #pragma unroll
       for (int s = 0; s < S; s++) {
@@ -721,7 +725,7 @@ static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct MixedLayout {
   long long K, K_pad;
-  int N, R, R_pad, nT, nTv, nC, nitems, npair, nkb, nsplit, kb_per_split, wb;
+  int N, R, R_pad, nT, nTv, nC, nitems, npair, nkb, nsplit, kb_per_split, wb, wbp;
   size_t off_adig, off_bdig, off_tmax, off_wpair, off_rmax, off_eA, off_fB, off_out, total;
 };
 
@@ -797,14 +801,18 @@ static MixedLayout mixed_layout(int nb1, int nb2, int nkp, int npb, int wb, int 
   L.kb_per_split = (L.nkb + L.nsplit - 1) / L.nsplit;
   L.nsplit = (L.nkb + L.kb_per_split - 1) / L.kb_per_split;   // no empty split
   L.wb = wb;
+  // B digits are prepared for at least two frequencies per pass over the A
+  // digits (each pass reads all five A planes), while the GEMM may take one
+  // frequency per launch
+  L.wbp = wb < 2 ? 2 : wb;
   size_t o = 0;
   L.off_adig = o; o += al256((size_t)S * L.R_pad * L.K_pad * 2);
-  L.off_bdig = o; o += al256((size_t)wb * S * L.R_pad * L.K_pad * 2);
+  L.off_bdig = o; o += al256((size_t)L.wbp * S * L.R_pad * L.K_pad * 2);
   L.off_tmax = o; o += al256((size_t)L.R_pad * L.nkb * 4);
-  L.off_wpair = o; o += al256((size_t)wb * L.K_pad * 8);
-  L.off_rmax = o; o += al256((size_t)wb * L.R_pad * 4);     // row maxima of |V·c·w| (float bits)
+  L.off_wpair = o; o += al256((size_t)L.wbp * L.K_pad * 8);
+  L.off_rmax = o; o += al256((size_t)L.wbp * L.R_pad * 4);  // row maxima of |V·c·w| (float bits)
   L.off_eA = o; o += al256((size_t)L.R_pad * 4);
-  L.off_fB = o; o += al256((size_t)wb * L.R_pad * 4);
+  L.off_fB = o; o += al256((size_t)L.wbp * L.R_pad * 4);
   L.off_out = o; o += al256((size_t)L.nsplit * wb * L.npair * TM * TM * 8);
   L.total = o;
   return L;
@@ -883,7 +891,7 @@ static int chi0_mixed_impl(const void* minm, int nkp, int k0, const int* kstart,
 
   CUtensorMap mapA, mapB;
   if (!make_map(&mapA, adig, L.R_pad, (long long)S * L.nkb)) return PG_ECUDA;
-  if (!make_map(&mapB, bdig, L.R_pad, (long long)wb * S * L.nkb)) return PG_ECUDA;
+  if (!make_map(&mapB, bdig, L.R_pad, (long long)L.wbp * S * L.nkb)) return PG_ECUDA;
   const size_t smem = gemm_smem_bytes();
   if (cudaFuncSetAttribute(k_ozaki_gemm<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return PG_ECUDA;
@@ -896,35 +904,45 @@ static int chi0_mixed_impl(const void* minm, int nkp, int k0, const int* kstart,
   attr[0].val.clusterDim.x = CL;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
-  for (int om0 = 0; om0 < nom; om0 += wb) {
-    const int nw = (om0 + wb <= nom) ? wb : nom - om0;
-    k_weights_prep<<<dim3(L.nkb, nw), 64, 0, s>>>(kcw, nb1, nb2, nkp_total, k0, nkp, kstart, knb2, om0, nw, coef,
-                                                  L.K, L.K_pad, wpair);
-    if (cudaMemsetAsync(rmax, 0, (size_t)L.wb * L.R_pad * 4, s) != cudaSuccess) return PG_ECUDA;
+  op.wl0 = 0;
+  const int wbp = L.wbp;
+  for (int op0 = 0; op0 < nom; op0 += wbp) {
+    // B digits of the frequencies op0 … op0+npw−1: one pass over the A digits
+    const int npw = (op0 + wbp <= nom) ? wbp : nom - op0;
+    k_weights_prep<<<dim3(L.nkb, npw), 64, 0, s>>>(kcw, nb1, nb2, nkp_total, k0, nkp, kstart, knb2, op0, npw, coef,
+                                                   L.K, L.K_pad, wpair);
+    if (cudaMemsetAsync(rmax, 0, (size_t)wbp * L.R_pad * 4, s) != cudaSuccess) return PG_ECUDA;
     k_rowmax_B<<<dim3((unsigned)((L.K_pad + 1023) / 1024), L.R_pad), 256, 0, s>>>(adig, wpair, L.R, L.R_pad, L.K_pad,
-                                                                                  nw, rmax);
-    k_row_exp_B<<<(nw * L.R_pad + 255) / 256, 256, 0, s>>>(rmax, eA, L.R, L.R_pad, nw, fB);
+                                                                                  npw, rmax);
+    k_row_exp_B<<<(npw * L.R_pad + 255) / 256, 256, 0, s>>>(rmax, eA, L.R, L.R_pad, npw, fB);
     k_digits_B<<<dim3((unsigned)((L.K_pad + 1023) / 1024), L.R_pad), 256, 0, s>>>(adig, eA, wpair, fB, L.R, L.R_pad,
-                                                                                  L.K_pad, nw, bdig);
-    cudaLaunchConfig_t cfg = {};
-    op.nw = nw;
-    // one cluster per unit: the hardware schedules the units in waves, whose
-    // staggered starts spread the digit traffic over time (a grid of
-    // co-resident clusters looping over the units measured 12 % slower at C3)
-    const int nunits = L.nitems * nw * L.nsplit;
-    cfg.gridDim = dim3((unsigned)(CL * nunits), 1, 1);
-    cfg.blockDim = dim3(NTHREADS);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    const int batch = om0 / wb;
-    if (gemm_events && cudaEventRecord((cudaEvent_t)gemm_events[2 * batch], s) != cudaSuccess) return PG_ECUDA;
-    if (cudaLaunchKernelEx(&cfg, k_ozaki_gemm<S>, mapA, mapB, op) != cudaSuccess) return PG_ECUDA;
-    if (gemm_events && cudaEventRecord((cudaEvent_t)gemm_events[2 * batch + 1], s) != cudaSuccess) return PG_ECUDA;
-    k_assemble<<<dim3((npb + 127) / 128, npb, nw), 128, 0, s>>>(out, eA, fB, npb, L.R_pad, L.nT, L.npair, L.nsplit,
-                                                               wb, om0, accumulate, (double2*)eps);
-    pg_count_launches(6);
+                                                                                  L.K_pad, npw, bdig);
+    pg_count_launches(4);
+    for (int g0 = 0; g0 < npw; g0 += wb) {
+      const int nw = (g0 + wb <= npw) ? wb : npw - g0;
+      const int om0 = op0 + g0;
+      cudaLaunchConfig_t cfg = {};
+      op.nw = nw;
+      op.wl0 = g0;
+      // one cluster per unit: the hardware schedules the units in waves, whose
+      // staggered starts spread the digit traffic over time (a grid of
+      // co-resident clusters looping over the units measured 12 % slower at C3)
+      const int nunits = L.nitems * nw * L.nsplit;
+      cfg.gridDim = dim3((unsigned)(CL * nunits), 1, 1);
+      cfg.blockDim = dim3(NTHREADS);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = s;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      const int batch = om0 / wb;
+      if (gemm_events && cudaEventRecord((cudaEvent_t)gemm_events[2 * batch], s) != cudaSuccess) return PG_ECUDA;
+      if (cudaLaunchKernelEx(&cfg, k_ozaki_gemm<S>, mapA, mapB, op) != cudaSuccess) return PG_ECUDA;
+      if (gemm_events && cudaEventRecord((cudaEvent_t)gemm_events[2 * batch + 1], s) != cudaSuccess) return PG_ECUDA;
+      k_assemble<<<dim3((npb + 127) / 128, npb, nw), 128, 0, s>>>(out, eA, fB + (size_t)g0 * L.R_pad, npb, L.R_pad,
+                                                                 L.nT, L.npair, L.nsplit, wb, om0, accumulate,
+                                                                 (double2*)eps);
+      pg_count_launches(2);
+    }
   }
   return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ECUDA;
 }
