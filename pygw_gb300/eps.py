@@ -104,7 +104,17 @@ def chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=None, k_chunk=Non
     if pm_k is not None and epsw1 is None:
         epsw1 = torch.zeros((nom, npb), dtype=torch.complex128, device="cuda")
     on_device = isinstance(minm, torch.Tensor) and minm.is_cuda
-    if on_device:
+    # Pinned host matrix elements for the split-precision contraction are
+    # staged whole when they fit: one copy, started while the weights kernel
+    # may still be running, then one pass over all k (per-chunk passes repeat
+    # the digit preparation and run shorter GEMM launches).
+    staged = False
+    if not on_device and k_chunk is None and precision == "mixed" and isinstance(minm, torch.Tensor):
+        free, _ = torch.cuda.mem_get_info()
+        wb_all = mixed_omega_batch(nb1, nb2, nkp, npb, nom)
+        need = nkp * P * npb * 16 + lib.pg_chi0_mixed_workspace(nb1, nb2, nkp, npb, wb_all, 0)
+        staged = need <= 0.8 * free
+    if on_device or staged:
         k_chunk = nkp                    # resident: one pass over all k
     elif k_chunk is None:
         # the tensor-core contraction wants long K per launch: bigger chunks
@@ -127,6 +137,21 @@ def chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=None, k_chunk=Non
     if on_device:
         m = minm.reshape(nkp, P, npb)
         _launch_chi0(lib, m, nkp, 0, kcw_d, nb1, nb2, nkp, nom, npb, eps, pm_chunk(0, nkp), epsw1, stream, timers,
+                     precision, mctx)
+        return eps, epsw1
+
+    if staged:
+        copy_stream = torch.cuda.Stream()
+        # allocated on the copy stream: its memory is none that kernels still
+        # queued on the compute stream use, so the copy need not wait for them
+        with torch.cuda.stream(copy_stream):
+            dev = torch.empty((nkp, P, npb), dtype=torch.complex128, device="cuda")
+            dev.copy_(minm.reshape(nkp, P, npb), non_blocking=True)
+            done = torch.cuda.Event()
+            done.record(copy_stream)
+        dev.record_stream(cur)
+        cur.wait_event(done)
+        _launch_chi0(lib, dev, nkp, 0, kcw_d, nb1, nb2, nkp, nom, npb, eps, pm_chunk(0, nkp), epsw1, stream, timers,
                      precision, mctx)
         return eps, epsw1
 

@@ -147,7 +147,8 @@ def test_mixed_q0_wings_and_head():
 
 def test_mixed_streamed_chunks_match_resident():
     """k-chunked split-precision χ0 (callable and pinned-host inputs, several
-    chunks, q→0 wings) against the one-pass contraction over resident k."""
+    chunks, q→0 wings) and the staged pinned-host path against the one-pass
+    contraction over resident k."""
     w = syn.scaled(syn.WORKLOADS["C1"], div=3, npb=96, nom=4)
     p, kcw, minm = _problem(w)
     nb1, nb2, nkp, nom = kcw.shape
@@ -160,7 +161,8 @@ def test_mixed_streamed_chunks_match_resident():
     assert int(status.item()) == 0
     ref = eps_all.cpu().numpy().transpose(2, 1, 0)
     host = torch.from_numpy(np.stack([m.reshape(P, N) for m in minm])).pin_memory()
-    for src, kc in ((lambda ik: minm[ik], 3), (host, 4)):
+    # (host, None): pinned host input staged whole on a copy stream, one pass
+    for src, kc in ((lambda ik: minm[ik], 3), (host, 4), (host, None)):
         st = torch.zeros(1, dtype=torch.int32, device="cuda")
         eps, w1 = peps.chi0_accumulate(kd, src, nkp, N, nb1, nb2, nom, pm_k=lambda ik: pms[ik], k_chunk=kc,
                                        precision="mixed", status=st)
