@@ -148,8 +148,8 @@ __global__ void __launch_bounds__(256) k_rows_digits(const double2* __restrict__
   }
 }
 
-// mwm from the digit-GEMM tiles: C[r,J] = G[r][J] + i·G[R+r][J], each scaled by
-// 2^(eA + fB − 16); mwm = wkq·Σ_J C[r,J]·M[r,J].  Thread per (row, frequency).
+// mwm from the digit-GEMM tiles: C[r,J] = (G[r][J] + i·G[R+r][J])·2^(eA[r] + fB[J] − 16),
+// mwm = wkq·Σ_J C[r,J]·M[r,J].  Thread per (row, frequency).
 __global__ void k_mwm_reduce(const double* __restrict__ out, const int* eA, const int* fB,
                              const double2* __restrict__ M, long long R, int N, int R_padB, int nTb, int ntile, int P,
                              int nom, int om0, double wkq, double2* __restrict__ mwm) {
@@ -157,21 +157,25 @@ __global__ void k_mwm_reduce(const double* __restrict__ out, const int* eA, cons
   const int wl = blockIdx.y;
   if (r >= R) return;
   const long long ri = R + r;
-  const int ea = eA[r], eai = eA[ri];
   const double* tr = out + ((size_t)wl * ntile + (size_t)(r >> 7) * nTb) * 16384 + (r & 127);
   const double* ti = out + ((size_t)wl * ntile + (size_t)(ri >> 7) * nTb) * 16384 + (ri & 127);
   const int* f = fB + (size_t)R_padB * wl;
   const double2* m = M + (size_t)r * N;
+  // rows r and R + r share the exponent eA[r]; the column factor 2^fB[J] is an
+  // exact power of two built from its bits (FP64 runs at a small fraction of
+  // the FP32 rate here, so the loop keeps to three FP64 operations per part)
   double sx = 0.0, sy = 0.0;
   for (int J = 0; J < N; J++) {
     const size_t o = (size_t)(J >> 7) * 16384 + (size_t)(J & 127) * 128;
-    const double cr = ldexp(tr[o], ea + f[J] - 16), ci = ldexp(ti[o], eai + f[J] - 16);
+    const double sJ = __hiloint2double((f[J] + 1023) << 20, 0);
+    const double gr = tr[o], gi = ti[o];
     const double2 v = m[J];
-    sx += cr * v.x - ci * v.y;
-    sy += cr * v.y + ci * v.x;
+    sx = fma(sJ, fma(gr, v.x, -gi * v.y), sx);
+    sy = fma(sJ, fma(gr, v.y, gi * v.x), sy);
   }
+  const double sc = wkq * ldexp(1.0, eA[r] - 16);
   const long long k = r / P, p = r - k * P;
-  mwm[((size_t)k * nom + om0 + wl) * P + p] = make_double2(wkq * sx, wkq * sy);
+  mwm[((size_t)k * nom + om0 + wl) * P + p] = make_double2(sc * sx, sc * sy);
 }
 
 // q = 0 (pygw.py:3358-3363): for each GW band row ie1 the pair (ie1, ie1 + off)
