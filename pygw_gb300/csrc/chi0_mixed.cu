@@ -65,7 +65,8 @@ constexpr uint32_t TMEM_COLS = 512;               // two 256-column low accumula
 constexpr unsigned long long WAIT_NS = 5000000000ull;   // 5 s per wait
 
 struct OzParams {
-  double* out;          // [nsplit][wb][npair][128 (col)][128 (row)]
+  double* out;          // [nsplit][wb][npair][128 (col)][128 (row)]: FP64, or in the general
+                        // product float pairs (hi, lo) whose sum is the value (see df_add2)
   unsigned* status;
   int R_pad, nT, nTv, nC, npair, nkb, kb_per_split, nsplit, wb;
   // general (full, non-symmetric) product: A digits per frequency, B with its own rows
@@ -211,6 +212,25 @@ __host__ __device__ constexpr uint32_t idesc_m128(int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
 }
 
+// (v.x + v.y) + a + b as a normalised float pair (hi, lo) by Knuth's two-sum:
+// with a, b exact (group integers times 2^-8d) the pair holds the running
+// tile value to ≈ 2^-47 relative, with FP32 operations only (FP64 runs at a
+// small fraction of the FP32 rate on this GPU, and the general product's short
+// K leaves the epilogue's group ends on the critical path).  The _rn
+// intrinsics keep the compiler from fusing products into the sums.
+__device__ __forceinline__ void two_sum_rn(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ float2 df_add2(float2 v, float a, float b) {
+  float s1, e1, s2, e2, x, y;
+  two_sum_rn(v.x, a, s1, e1);
+  two_sum_rn(s1, b, s2, e2);
+  two_sum_rn(s2, __fadd_rn(__fadd_rn(e1, e2), v.y), x, y);
+  return make_float2(x, y);
+}
+
 // Linear index → (i, j), i ≤ j < n, row-major over the upper triangle.
 __host__ __device__ __forceinline__ void tri_pair(int lin, int n, int& i, int& j) {
   int t = 0, rem = lin;
@@ -238,7 +258,7 @@ __device__ __forceinline__ void load_coords(const OzParams& p, int i, int nkbs, 
 // ------------------------------------------------------ the digit GEMM
 // SD digits per value; digit pairs s + t ≤ SD − 1 (SD = 5 for χ0, 6 for the
 // residual of the ε⁻¹ refinement).
-template <int SD>
+template <int SD, bool DF>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_ozaki_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -432,18 +452,37 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             // 8 columns at a time keep the live registers to hi[] + 16
             const bool used0 = nchunks_group >= 2 || (c_first & 1) == 0;
             const bool used1 = nchunks_group >= 2 || (c_first & 1) == 1;
-            const double scale = ldexp(1.0, -8 * d);
+            if constexpr (!DF) {
+              const double scale = ldexp(1.0, -8 * d);
 #pragma unroll
-            for (int cc = 0; cc < TM / 8; cc++) {
-              float l0[8], l1[8];
-              if (used0) tmem_ld8(t_b0 + cc * 8, l0);
-              if (used1) tmem_ld8(t_b1 + cc * 8, l1);
+              for (int cc = 0; cc < TM / 8; cc++) {
+                float l0[8], l1[8];
+                if (used0) tmem_ld8(t_b0 + cc * 8, l0);
+                if (used1) tmem_ld8(t_b1 + cc * 8, l1);
 #pragma unroll
-              for (int i = 0; i < 8; i++) {
-                const float r = (used0 ? l0[i] : 0.0f) + (used1 ? l1[i] : 0.0f);
-                const double v = (double)hi[cc * 8 + i] + (double)r;
-                double& o = out[(size_t)(cc * 8 + i) * TM + row];
-                o = (d == 0) ? v * scale : o + v * scale;
+                for (int i = 0; i < 8; i++) {
+                  const float r = (used0 ? l0[i] : 0.0f) + (used1 ? l1[i] : 0.0f);
+                  const double v = (double)hi[cc * 8 + i] + (double)r;
+                  double& o = out[(size_t)(cc * 8 + i) * TM + row];
+                  o = (d == 0) ? v * scale : o + v * scale;
+                }
+              }
+            } else {
+              // float-pair tile: hi·2^-8d and r·2^-8d are exact floats
+              float2* out2 = reinterpret_cast<float2*>(out);
+              const float fscale = __int_as_float((127 - 8 * d) << 23);
+#pragma unroll
+              for (int cc = 0; cc < TM / 8; cc++) {
+                float l0[8], l1[8];
+                if (used0) tmem_ld8(t_b0 + cc * 8, l0);
+                if (used1) tmem_ld8(t_b1 + cc * 8, l1);
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                  const float r = __fadd_rn(used0 ? l0[i] : 0.0f, used1 ? l1[i] : 0.0f);
+                  float2& o = out2[(size_t)(cc * 8 + i) * TM + row];
+                  const float2 prev = (d == 0) ? make_float2(0.0f, 0.0f) : o;
+                  o = df_add2(prev, __fmul_rn(hi[cc * 8 + i], fscale), __fmul_rn(r, fscale));
+                }
               }
             }
           }
@@ -753,9 +792,9 @@ static int gemm_cta_capacity() {
   cfg.dynamicSmemBytes = gemm_smem_bytes();
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (cudaFuncSetAttribute(k_ozaki_gemm<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes()) !=
+  if (cudaFuncSetAttribute(k_ozaki_gemm<S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes()) !=
           cudaSuccess ||
-      cudaOccupancyMaxActiveClusters(&ncl, k_ozaki_gemm<S>, &cfg) != cudaSuccess || ncl <= 0) {
+      cudaOccupancyMaxActiveClusters(&ncl, k_ozaki_gemm<S, false>, &cfg) != cudaSuccess || ncl <= 0) {
     cudaGetLastError();
     int sms = 148;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -893,7 +932,7 @@ static int chi0_mixed_impl(const void* minm, int nkp, int k0, const int* kstart,
   if (!make_map(&mapA, adig, L.R_pad, (long long)S * L.nkb)) return PG_ECUDA;
   if (!make_map(&mapB, bdig, L.R_pad, (long long)L.wbp * S * L.nkb)) return PG_ECUDA;
   const size_t smem = gemm_smem_bytes();
-  if (cudaFuncSetAttribute(k_ozaki_gemm<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_ozaki_gemm<S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return PG_ECUDA;
   OzParams op;
   op.out = out; op.status = d_status; op.R_pad = L.R_pad; op.nT = L.nT; op.nTv = L.nTv; op.nC = L.nC;
@@ -936,7 +975,7 @@ static int chi0_mixed_impl(const void* minm, int nkp, int k0, const int* kstart,
       cfg.numAttrs = 1;
       const int batch = om0 / wb;
       if (gemm_events && cudaEventRecord((cudaEvent_t)gemm_events[2 * batch], s) != cudaSuccess) return PG_ECUDA;
-      if (cudaLaunchKernelEx(&cfg, k_ozaki_gemm<S>, mapA, mapB, op) != cudaSuccess) return PG_ECUDA;
+      if (cudaLaunchKernelEx(&cfg, k_ozaki_gemm<S, false>, mapA, mapB, op) != cudaSuccess) return PG_ECUDA;
       if (gemm_events && cudaEventRecord((cudaEvent_t)gemm_events[2 * batch + 1], s) != cudaSuccess) return PG_ECUDA;
       k_assemble<<<dim3((npb + 127) / 128, npb, nw), 128, 0, s>>>(out, eA, fB + (size_t)g0 * L.R_pad, npb, L.R_pad,
                                                                  L.nT, L.npair, L.nsplit, wb, om0, accumulate,
@@ -982,7 +1021,7 @@ int pgm::launch_gemm_general(const __nv_bfloat16* adig, const __nv_bfloat16* bdi
   if (!make_map(&mapA, (void*)adig, R_padA, (long long)(a_per_w ? nw : 1) * sd * nkb)) return PG_ECUDA;
   if (!make_map(&mapB, (void*)bdig, R_padB, (long long)nw * sd * nkb)) return PG_ECUDA;
   const size_t smem = gemm_smem_bytes();
-  auto kern = (sd == 6) ? k_ozaki_gemm<6> : k_ozaki_gemm<5>;
+  auto kern = (sd == 6) ? k_ozaki_gemm<6, true> : k_ozaki_gemm<5, true>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return PG_ECUDA;
   OzParams op;

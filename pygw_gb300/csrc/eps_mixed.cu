@@ -286,10 +286,11 @@ __global__ void k_residual(const double* __restrict__ out, const int* eA, const 
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y, w = blockIdx.z;
   if (i >= N) return;
+  const float2* out2 = reinterpret_cast<const float2*>(out);      // float-pair tiles
   auto G = [&](int r, int c) -> double {
     const int tile = (r >> 7) * nTb + (c >> 7);
-    const double v = out[((size_t)w * ntile + tile) * 16384 + (size_t)(c & 127) * 128 + (r & 127)];
-    return ldexp(v, eA[(size_t)R_padA * w + r] + fB[(size_t)R_padB * w + c] - 16);
+    const float2 t = out2[((size_t)w * ntile + tile) * 16384 + (size_t)(c & 127) * 128 + (r & 127)];
+    return ldexp((double)t.x + (double)t.y, eA[(size_t)R_padA * w + r] + fB[(size_t)R_padB * w + c] - 16);
   };
   const double re = G(i, j), im = G(N + i, j);
   R[(size_t)N * N * w + (size_t)N * j + i] = make_double2((i == j ? 1.0 : 0.0) - re, -im);

@@ -38,7 +38,8 @@ __device__ __forceinline__ int row_exponent(float bound) {
 // per value and digit pairs s + t ≤ sd − 1 (A digits per frequency, R_padA × K,
 // B digits R_padB × K, K = 64·nkb, one K split; sd = 6 takes the result from
 // ≈ 2^-40 to ≈ 2^-48 of the row scales).
-// out: [nw][R_padA/128 · R_padB/128 tiles][128 (col)][128 (row)] FP64.
+// out: [nw][R_padA/128 · R_padB/128 tiles][128 (col)][128 (row)] float pairs
+// (hi, lo), 8 bytes per element; an element's value is (double)hi + (double)lo.
 // nTbv: B tiles holding real rows.  Returns a PG_* code.
 // a_per_w: A digits per frequency (1) or one set shared by the frequencies (0).
 int launch_gemm_general(const __nv_bfloat16* adig, const __nv_bfloat16* bdig, int sd, int a_per_w, int R_padA,

@@ -157,8 +157,9 @@ __global__ void k_mwm_reduce(const double* __restrict__ out, const int* eA, cons
   const int wl = blockIdx.y;
   if (r >= R) return;
   const long long ri = R + r;
-  const double* tr = out + ((size_t)wl * ntile + (size_t)(r >> 7) * nTb) * 16384 + (r & 127);
-  const double* ti = out + ((size_t)wl * ntile + (size_t)(ri >> 7) * nTb) * 16384 + (ri & 127);
+  const float2* out2 = reinterpret_cast<const float2*>(out);      // float-pair tiles (hi, lo)
+  const float2* tr = out2 + ((size_t)wl * ntile + (size_t)(r >> 7) * nTb) * 16384 + (r & 127);
+  const float2* ti = out2 + ((size_t)wl * ntile + (size_t)(ri >> 7) * nTb) * 16384 + (ri & 127);
   const int* f = fB + (size_t)R_padB * wl;
   const double2* m = M + (size_t)r * N;
   // rows r and R + r share the exponent eA[r]; the column factor 2^fB[J] is an
@@ -168,7 +169,8 @@ __global__ void k_mwm_reduce(const double* __restrict__ out, const int* eA, cons
   for (int J = 0; J < N; J++) {
     const size_t o = (size_t)(J >> 7) * 16384 + (size_t)(J & 127) * 128;
     const double sJ = __hiloint2double((f[J] + 1023) << 20, 0);
-    const double gr = tr[o], gi = ti[o];
+    const float2 pr = tr[o], pi = ti[o];
+    const double gr = (double)pr.x + (double)pr.y, gi = (double)pi.x + (double)pi.y;
     const double2 v = m[J];
     sx = fma(sJ, fma(gr, v.x, -gi * v.y), sx);
     sy = fma(sJ, fma(gr, v.y, gi * v.x), sy);
