@@ -1,5 +1,10 @@
 """numpy restatement of the χ0 contraction and ε⁻¹ (test infrastructure).
 
+Parity unpinned: the reference ships no tests, fixtures or golden vectors for this
+path and cannot be built or run here (Fortran without a compiler, Python 2 with
+f2py modules); this restatement is pinned by known answers instead
+(tests/test_oracle_*.py).
+
 Follows MatrixElements2Band.calc_eps (pygw.py:3039-3297) for a Γ-point or
 finite q, with or without the SVD frequency basis:
 

@@ -1,5 +1,10 @@
 """Independent quadrature of the tetrahedron weight integral (test infrastructure).
 
+Parity unpinned: the reference ships no tests, fixtures or golden vectors for this
+path and cannot be built or run here (Fortran without a compiler, Python 2 with
+f2py modules); this restatement is pinned by known answers instead
+(tests/test_oracle_*.py).
+
 Restates the integrand of ``stweight_numeric`` (for_tetrahedra2.f90:1504-1604,
 ``iop_omg = 1``): for the unit tetrahedron with energy differences ``de`` at
 its corners,

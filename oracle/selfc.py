@@ -1,5 +1,10 @@
 """numpy restatement of the correlation self-energy contraction (test infrastructure).
 
+Parity unpinned: the reference ships no tests, fixtures or golden vectors for this
+path and cannot be built or run here (Fortran without a compiler, Python 2 with
+f2py modules); this restatement is pinned by known answers instead
+(tests/test_oracle_*.py).
+
 Follows MatrixElements2Band.calc_selfc (pygw.py:3299-3412) for one q and the
 frequency convolution it calls (mcommon.py:80-131 → fnc.f90:90-177):
 

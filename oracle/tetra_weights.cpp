@@ -1,5 +1,9 @@
 // ORACLE — test infrastructure only, never part of the product path.
 //
+// Parity unpinned: the reference ships no tests, fixtures or golden vectors for
+// this path and its Fortran cannot be built here (no Fortran compiler); this
+// restatement is pinned by known answers instead (tests/test_oracle_weights.py).
+//
 // CPU restatement of PyGW's imaginary-axis tetrahedron polarization weights
 // (the routine PyGW calls as ft.bz_calcqdepw_par2, pygw.py:3443), written to
 // follow the reference's control flow, thresholds and left-to-right arithmetic:

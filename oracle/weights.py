@@ -1,5 +1,10 @@
 """ctypes front end of the oracle's weight restatement (test infrastructure).
 
+Parity unpinned: the reference ships no tests, fixtures or golden vectors for this
+path and cannot be built or run here (Fortran without a compiler, Python 2 with
+f2py modules); this restatement is pinned by known answers instead
+(tests/test_oracle_*.py).
+
 ``bz_calcqdepw_par2`` mirrors the f2py call of the reference
 (``kcw = ft.bz_calcqdepw_par2(enk, ef, kqid, ncg, nomx, numin, omega, tetc)``,
 pygw.py:3443, for_tetrahedra.f90:390): array sizes are inferred from the
