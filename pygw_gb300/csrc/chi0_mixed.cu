@@ -28,11 +28,11 @@
 // tile of the block is loaded half by each CTA and multicast to both, so each
 // SM reads 32 KB from L2 per 64-wide K-block for 2·128·256·64 flop.
 // Warp 0 issues the TMA loads (A tile + two B halves per stage, 128-byte
-// swizzle, 4 stages), warp 1 allocates TMEM and issues the MMAs, warps 2–9
+// swizzle, 4 stages), warp 1 allocates TMEM and issues the MMAs, warps 2 …
 // renormalise: the low accumulators (two 256-column TMEM buffers used in
 // turn, so the tensor core keeps working while the previous chunk is
 // renormalised) and a high accumulator per group held in registers (each
-// epilogue thread owns one row × 128 columns).  A stage is refilled only when
+// epilogue thread owns one row × 128 or × 64 columns, see epi_warps).  A stage is refilled only when
 // the MMAs of both CTAs have read it (each MMA commit arrives on both CTAs'
 // "empty" barriers).  Every wait is bounded (≈ 5 s of %globaltimer); on
 // expiry the kernel records PG_ERR_TIMEOUT, drains its own in-flight work,
@@ -59,8 +59,13 @@ constexpr int LBLK = 14;        // K-blocks per exact chunk: 14·64·129² + 2^1
 constexpr int CL = 2;           // CTAs per cluster (share the B tile)
 constexpr int TILE_BYTES = TM * KB * 2;           // 16 KB: one 128-row digit tile
 constexpr int STAGE_BYTES = 3 * TILE_BYTES;       // A tile + the two B halves
-constexpr int NEPI = 8;                           // epilogue warps
-constexpr int NTHREADS = 32 * (2 + NEPI);         // 320
+// Epilogue warps: 8 (each thread one row × 128 columns) for the symmetric χ0
+// product, whose long K hides the epilogue behind the MMAs; 16 (one row × 64
+// columns) for the general product, whose short K leaves the digit-group ends
+// on the critical path — half the registers per thread, more tile loads in
+// flight (C3 self-energy step 8.12 → 6.66 s; χ0 at C3 76.3 → 79.9 ms with 16).
+__host__ __device__ constexpr int epi_warps(bool general) { return general ? 16 : 8; }
+__host__ __device__ constexpr int gemm_threads(bool general) { return 32 * (2 + epi_warps(general)); }
 constexpr uint32_t TMEM_COLS = 512;               // two 256-column low accumulators
 constexpr unsigned long long WAIT_NS = 5000000000ull;   // 5 s per wait
 
@@ -259,8 +264,10 @@ __device__ __forceinline__ void load_coords(const OzParams& p, int i, int nkbs, 
 // SD digits per value; digit pairs s + t ≤ SD − 1 (SD = 5 for χ0, 6 for the
 // residual of the ε⁻¹ refinement).
 template <int SD, bool DF>
-__global__ void __launch_bounds__(NTHREADS, 1)
+__global__ void __launch_bounds__(gemm_threads(DF), 1)
     k_ozaki_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p) {
+  constexpr int NEPI = epi_warps(DF);             // epilogue warps: NEPI/4 per TMEM lane quarter
+  constexpr int CW = TN / (NEPI / 4);             // columns per epilogue thread
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + NST * STAGE_BYTES);
@@ -404,13 +411,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       while (!mbar_test(drain, 0) && gtime() - t0 < WAIT_NS) {}
     }
   } else {
-    // ---------------------------------------------------------- epilogue (warps 2–9)
+    // ---------------------------------------------------------- epilogue (warps 2 … 2+NEPI−1)
     const int q = warp & 3;                        // TMEM lane quarter this warp may access
-    const int h = (warp - 2) >> 2;                 // column half of the block
+    const int sl = (warp - 2) >> 2;                // column slice of the block (CW columns)
+    const int h = (sl * CW) / TM;                  // its 128-column tile of the block
+    const int co = (sl * CW) % TM;                 // its first column within that tile
     const int row = q * 32 + lane;                 // accumulator row (A tile row)
-    const uint32_t t_b0 = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * TM);
+    const uint32_t t_b0 = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(sl * CW);
     const uint32_t t_b1 = t_b0 + TN;
-    float hi[TM];                                  // high accumulator: multiples of 2^12, exact below 2^36
+    float hi[CW];                                  // high accumulator: multiples of 2^12, exact below 2^36
     int c = 0;
     bool ok = true;
     for (int u = cid; u < nunits && ok; u += ncl) {
@@ -423,7 +432,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const int nchunk_per_pass = (U.kb1 - U.kb0 + LBLK - 1) / LBLK;
       for (int d = 0; d < SD && ok; d++) {
 #pragma unroll
-        for (int i = 0; i < TM; i++) hi[i] = 0.0f;
+        for (int i = 0; i < CW; i++) hi[i] = 0.0f;
         const int nchunks_group = (d + 1) * nchunk_per_pass;
         const int c_first = c;
         for (int gc = 0; gc < nchunks_group && ok; gc++, c++) {
@@ -434,7 +443,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           if (active) {
             const uint32_t tl = b ? t_b1 : t_b0;
 #pragma unroll
-            for (int cc = 0; cc < TM / 16; cc++) {
+            for (int cc = 0; cc < CW / 16; cc++) {
               float lo[16];
               tmem_ld16(tl + cc * 16, lo);
 #pragma unroll
@@ -455,7 +464,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             if constexpr (!DF) {
               const double scale = ldexp(1.0, -8 * d);
 #pragma unroll
-              for (int cc = 0; cc < TM / 8; cc++) {
+              for (int cc = 0; cc < CW / 8; cc++) {
                 float l0[8], l1[8];
                 if (used0) tmem_ld8(t_b0 + cc * 8, l0);
                 if (used1) tmem_ld8(t_b1 + cc * 8, l1);
@@ -463,7 +472,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 for (int i = 0; i < 8; i++) {
                   const float r = (used0 ? l0[i] : 0.0f) + (used1 ? l1[i] : 0.0f);
                   const double v = (double)hi[cc * 8 + i] + (double)r;
-                  double& o = out[(size_t)(cc * 8 + i) * TM + row];
+                  double& o = out[(size_t)(co + cc * 8 + i) * TM + row];
                   o = (d == 0) ? v * scale : o + v * scale;
                 }
               }
@@ -472,14 +481,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               float2* out2 = reinterpret_cast<float2*>(out);
               const float fscale = __int_as_float((127 - 8 * d) << 23);
 #pragma unroll
-              for (int cc = 0; cc < TM / 8; cc++) {
+              for (int cc = 0; cc < CW / 8; cc++) {
                 float l0[8], l1[8];
                 if (used0) tmem_ld8(t_b0 + cc * 8, l0);
                 if (used1) tmem_ld8(t_b1 + cc * 8, l1);
 #pragma unroll
                 for (int i = 0; i < 8; i++) {
                   const float r = __fadd_rn(used0 ? l0[i] : 0.0f, used1 ? l1[i] : 0.0f);
-                  float2& o = out2[(size_t)(cc * 8 + i) * TM + row];
+                  float2& o = out2[(size_t)(co + cc * 8 + i) * TM + row];
                   const float2 prev = (d == 0) ? make_float2(0.0f, 0.0f) : o;
                   o = df_add2(prev, __fmul_rn(hi[cc * 8 + i], fscale), __fmul_rn(r, fscale));
                 }
@@ -492,9 +501,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
       }
       if (stored && !active) {
-        for (int i = 0; i < TM; i++) out[(size_t)i * TM + row] = 0.0;        // padding tile
+        for (int i = 0; i < CW; i++) out[(size_t)(co + i) * TM + row] = 0.0;        // padding tile
       } else if (stored && !ok) {
-        for (int i = 0; i < TM; i++) out[(size_t)i * TM + row] = __longlong_as_double(0x7ff8dead00000000LL);
+        for (int i = 0; i < CW; i++) out[(size_t)(co + i) * TM + row] = __longlong_as_double(0x7ff8dead00000000LL);
       }
     }
   }
@@ -788,7 +797,7 @@ static int gemm_cta_capacity() {
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.gridDim = dim3(CL, 1, 1);
-  cfg.blockDim = dim3(NTHREADS);
+  cfg.blockDim = dim3(gemm_threads(false));
   cfg.dynamicSmemBytes = gemm_smem_bytes();
   cfg.attrs = attr;
   cfg.numAttrs = 1;
@@ -968,7 +977,7 @@ static int chi0_mixed_impl(const void* minm, int nkp, int k0, const int* kstart,
       // co-resident clusters looping over the units measured 12 % slower at C3)
       const int nunits = L.nitems * nw * L.nsplit;
       cfg.gridDim = dim3((unsigned)(CL * nunits), 1, 1);
-      cfg.blockDim = dim3(NTHREADS);
+      cfg.blockDim = dim3(gemm_threads(false));
       cfg.dynamicSmemBytes = smem;
       cfg.stream = s;
       cfg.attrs = attr;
@@ -1038,7 +1047,7 @@ int pgm::launch_gemm_general(const __nv_bfloat16* adig, const __nv_bfloat16* bdi
   cudaLaunchConfig_t cfg = {};
   op.nw = nw;
   cfg.gridDim = dim3((unsigned)(CL * op.nC * op.nCb * nw), 1, 1);
-  cfg.blockDim = dim3(NTHREADS);
+  cfg.blockDim = dim3(gemm_threads(true));
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cfg.attrs = attr;
