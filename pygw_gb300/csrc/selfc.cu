@@ -104,9 +104,10 @@ __global__ void __launch_bounds__(256) k_mwm_f64(const double2* __restrict__ M, 
 // ------------------------------------------------------- split precision
 // Rows r and R + r of A = [[Re M, Im M], [−Im M, Re M]] (the real form of
 // conj(M), K = 2N): a shared exponent from max_I(|Re M|, |Im M|) and five
-// digits per value.  One block per row r.
+// digits per value; and X = M·2^-e as float pairs for the reduction.  One
+// block per row r.
 __global__ void __launch_bounds__(256) k_rows_digits(const double2* __restrict__ M, long long R, int N, int R_pad,
-                                                     int nkb, int* eA, __nv_bfloat16* adig) {
+                                                     int nkb, int* eA, __nv_bfloat16* adig, float4* X) {
   const long long r = blockIdx.x;
   const double2* row = M + (size_t)r * N;
   double m = 0.0;
@@ -133,6 +134,10 @@ __global__ void __launch_bounds__(256) k_rows_digits(const double2* __restrict__
   for (int I = threadIdx.x; I < N; I += blockDim.x) {
     const double2 x = row[I];
     double yr = ldexp(x.x, -e), yi = ldexp(x.y, -e);
+    // M[r][I]·2^-e as float pairs (hi = nearest float, lo = nearest float to the rest),
+    // column-major for the reduction's coalesced reads
+    const float xh = __double2float_rn(yr), yh = __double2float_rn(yi);
+    X[(size_t)I * R + r] = make_float4(xh, __double2float_rn(yr - (double)xh), yh, __double2float_rn(yi - (double)yh));
 #pragma unroll
     for (int s = 0; s < pgm::OZ_S; s++) {
       const double tr = yr * 256.0, ti = yi * 256.0;
@@ -148,36 +153,53 @@ __global__ void __launch_bounds__(256) k_rows_digits(const double2* __restrict__
   }
 }
 
-// mwm from the digit-GEMM tiles: C[r,J] = (G[r][J] + i·G[R+r][J])·2^(eA[r] + fB[J] − 16),
-// mwm = wkq·Σ_J C[r,J]·M[r,J].  Thread per (row, frequency).
+// (S, C) += (gh + gl)·(xh + xl)·s with s a power of two, in float-pair
+// arithmetic: the leading product exactly by FMA, the cross terms (≈ 2^-24 of
+// it) into the low part, the sum by Knuth's two-sum.  The _rn intrinsics keep
+// the compiler from fusing products into the sums.
+__device__ __forceinline__ void df_mac(float gh, float gl, float xh, float xl, float s, float& S, float& C) {
+  const float ah = __fmul_rn(gh, s), al = __fmul_rn(gl, s);          // exact
+  const float p = __fmul_rn(ah, xh);
+  float e = __fmaf_rn(ah, xh, -p);
+  e = __fmaf_rn(ah, xl, e);
+  e = __fmaf_rn(al, xh, e);
+  e = __fmaf_rn(al, xl, e);
+  const float t = __fadd_rn(S, p), b = __fsub_rn(t, S);
+  C = __fadd_rn(C, __fadd_rn(__fadd_rn(__fsub_rn(S, __fsub_rn(t, b)), __fsub_rn(p, b)), e));
+  S = t;
+}
+
+// mwm from the digit-GEMM tiles (float pairs): C[r,J] = (G[r][J] + i·G[R+r][J])·2^(eA[r] + fB[J] − 16),
+// mwm = wkq·Σ_J C[r,J]·M[r,J] = wkq·2^(2·eA[r] − 16)·Σ_J G·2^fB[J]·X[J][r] with X = M·2^-eA
+// (float pairs), summed in float-pair arithmetic: GB300's FP64 rate is a small
+// fraction of its FP32 rate, and FP64 is used once per row.  Thread per (row, frequency).
 __global__ void k_mwm_reduce(const double* __restrict__ out, const int* eA, const int* fB,
-                             const double2* __restrict__ M, long long R, int N, int R_padB, int nTb, int ntile, int P,
+                             const float4* __restrict__ X, long long R, int N, int R_padB, int nTb, int ntile, int P,
                              int nom, int om0, double wkq, double2* __restrict__ mwm) {
   const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int wl = blockIdx.y;
   if (r >= R) return;
   const long long ri = R + r;
-  const float2* out2 = reinterpret_cast<const float2*>(out);      // float-pair tiles (hi, lo)
+  const float2* out2 = reinterpret_cast<const float2*>(out);
   const float2* tr = out2 + ((size_t)wl * ntile + (size_t)(r >> 7) * nTb) * 16384 + (r & 127);
   const float2* ti = out2 + ((size_t)wl * ntile + (size_t)(ri >> 7) * nTb) * 16384 + (ri & 127);
   const int* f = fB + (size_t)R_padB * wl;
-  const double2* m = M + (size_t)r * N;
-  // rows r and R + r share the exponent eA[r]; the column factor 2^fB[J] is an
-  // exact power of two built from its bits (FP64 runs at a small fraction of
-  // the FP32 rate here, so the loop keeps to three FP64 operations per part)
-  double sx = 0.0, sy = 0.0;
+  float S1 = 0.0f, C1 = 0.0f, S2 = 0.0f, C2 = 0.0f;
   for (int J = 0; J < N; J++) {
     const size_t o = (size_t)(J >> 7) * 16384 + (size_t)(J & 127) * 128;
-    const double sJ = __hiloint2double((f[J] + 1023) << 20, 0);
-    const float2 pr = tr[o], pi = ti[o];
-    const double gr = (double)pr.x + (double)pr.y, gi = (double)pi.x + (double)pi.y;
-    const double2 v = m[J];
-    sx = fma(sJ, fma(gr, v.x, -gi * v.y), sx);
-    sy = fma(sJ, fma(gr, v.y, gi * v.x), sy);
+    const float2 gr = tr[o], gi = ti[o];
+    const float4 x = X[(size_t)J * R + r];
+    const float sJ = __int_as_float((f[J] + 127) << 23);
+    // Re += G_re·Re X − G_im·Im X,  Im += G_re·Im X + G_im·Re X
+    df_mac(gr.x, gr.y, x.x, x.y, sJ, S1, C1);
+    df_mac(-gi.x, -gi.y, x.z, x.w, sJ, S1, C1);
+    df_mac(gr.x, gr.y, x.z, x.w, sJ, S2, C2);
+    df_mac(gi.x, gi.y, x.x, x.y, sJ, S2, C2);
   }
-  const double sc = wkq * ldexp(1.0, eA[r] - 16);
+  const double sc = wkq * ldexp(1.0, 2 * eA[r] - 16);
   const long long k = r / P, p = r - k * P;
-  mwm[((size_t)k * nom + om0 + wl) * P + p] = make_double2(sc * sx, sc * sy);
+  mwm[((size_t)k * nom + om0 + wl) * P + p] =
+      make_double2(sc * ((double)S1 + (double)C1), sc * ((double)S2 + (double)C2));
 }
 
 // q = 0 (pygw.py:3358-3363): for each GW band row ie1 the pair (ie1, ie1 + off)
@@ -337,7 +359,7 @@ static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 struct MLayout {
   long long R;
   int N, nw, R_padA, R_padB, nkb, nTb, ntile;
-  size_t adig, bdig, eA, fB, out, total;
+  size_t adig, bdig, eA, fB, X, out, total;
 };
 static MLayout mlayout(long long R, int N, int nw) {
   MLayout L;
@@ -353,6 +375,7 @@ static MLayout mlayout(long long R, int N, int nw) {
   L.bdig = o; o += al256((size_t)2 * pgm::OZ_S * L.R_padB * K_pad * nw);
   L.eA = o; o += al256(sizeof(int) * (size_t)L.R_padA);
   L.fB = o; o += al256(sizeof(int) * (size_t)L.R_padB * nw);
+  L.X = o; o += al256(sizeof(float4) * (size_t)R * N);
   L.out = o; o += al256(sizeof(double) * (size_t)L.ntile * 16384 * nw);
   L.total = o;
   return L;
@@ -399,7 +422,8 @@ extern "C" int pg_selfc_mwm(const void* minm, int nk, int P, int npb, const void
   double* gout = (double*)(w + L.out);
   if (cudaMemsetAsync(adig, 0, (size_t)2 * pgm::OZ_S * L.R_padA * L.nkb * 64, s) != cudaSuccess) return PG_ECUDA;
   if (cudaMemsetAsync(eA, 0, sizeof(int) * (size_t)L.R_padA, s) != cudaSuccess) return PG_ECUDA;
-  k_rows_digits<<<(unsigned)R, 256, 0, s>>>(M, R, N, L.R_padA, L.nkb, eA, adig);
+  float4* X = (float4*)(w + L.X);
+  k_rows_digits<<<(unsigned)R, 256, 0, s>>>(M, R, N, L.R_padA, L.nkb, eA, adig, X);
   pg_count_launches(1);
   for (int om0 = 0; om0 < nom; om0 += nb) {
     const int nw = (om0 + nb <= nom) ? nb : nom - om0;
@@ -408,7 +432,7 @@ extern "C" int pg_selfc_mwm(const void* minm, int nk, int P, int npb, const void
     rc = pgm::launch_gemm_general(adig, bdig, pgm::OZ_S, 0, L.R_padA, L.R_padB, (N + 127) / 128, L.nkb, nw, gout,
                                   d_status, s);
     if (rc != PG_OK) return rc;
-    k_mwm_reduce<<<dim3((unsigned)((R + 127) / 128), nw), 128, 0, s>>>(gout, eA, fB, M, R, N, L.R_padB, L.nTb,
+    k_mwm_reduce<<<dim3((unsigned)((R + 127) / 128), nw), 128, 0, s>>>(gout, eA, fB, X, R, N, L.R_padB, L.nTb,
                                                                       L.ntile, P, nom, om0, wkq, out);
     pg_count_launches(1);
   }

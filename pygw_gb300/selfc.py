@@ -43,7 +43,7 @@ def _vec_device(a, nom, n=None):
 def mixed_k_chunk(P, npb, nom, budget=None):
     """(k-chunk, ω batch) whose split-precision workspace stays within the budget."""
     budget = WORK_BUDGET if budget is None else budget
-    per_row = 40 * npb + 16 * npb          # A digits + one frequency of tiles, per (k, p) row
+    per_row = 56 * npb + 16 * npb          # A digits and the float-pair copy of M + one frequency of tiles
     nk = max(1, int(budget // 2 // max(1, per_row * P)))
     lib = _lib.load()
     nb = nom
