@@ -1009,11 +1009,15 @@ __global__ void __launch_bounds__(128) k_tet_classify(Params p, long long nitems
   if (threadIdx.x < NCLASS && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
 }
 
-// Exclusive prefix of the class histogram → per-class write cursors.
+// Exclusive prefix of the class histogram → per-class write cursors, the
+// classes in descending order: the largest polyhedra (the most sub-tetrahedra
+// per item) run first and the items that contribute zero last, so the last
+// wave of blocks is short (ascending order left most SMs idle behind a tail
+// of 8-node items).
 __global__ void k_class_offsets(const unsigned* hist, unsigned* cursor) {
   if (threadIdx.x == 0) {
     unsigned acc = 0;
-    for (int c = 0; c < NCLASS; c++) { cursor[c] = acc; acc += hist[c]; }
+    for (int c = NCLASS - 1; c >= 0; c--) { cursor[c] = acc; acc += hist[c]; }
   }
 }
 
