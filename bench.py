@@ -59,6 +59,10 @@ def parse():
                     help="selfc: the correlation self-energy step (mwm contraction + Matsubara convolution) "
                          "on the workload's k mesh, N_PB and frequencies")
     ap.add_argument("--selfc-nb1", type=int, default=16, help="selfc: GW bands (nbgw - ibgw)")
+    ap.add_argument("--omega-batch", type=int, default=0,
+                    help="mixed chi0: frequencies per digit-GEMM launch (0: the library's rule)")
+    ap.add_argument("--kb-split", type=int, default=0,
+                    help="mixed chi0: K-blocks per K split of the digit GEMM (0: automatic)")
     return ap.parse_args()
 
 
@@ -198,7 +202,7 @@ def gpu_step(inp, step, timers=None, stream=None, precision="fp64", phases=None)
         ev[1].record(cs)
     if precision == "mixed":
         eps, status, inp.mwork = peps.chi0_mixed(r.kcw, inp.minm_dev, inp.nkp, inp.w.npb, inp.nb1, inp.nb2,
-                                                 inp.w.nom, omega_batch=inp.wb, stream=stream,
+                                                 inp.w.nom, omega_batch=inp.wb, kb_split=inp.kb_split, stream=stream,
                                                  work=getattr(inp, "mwork", None), timers=timers,
                                                  gemm_timers=inp.gemm_timers if timers is not None else None)
         inp.statuses.append(status)
@@ -737,7 +741,8 @@ def main():
     inp.gemm_timers = []
     if a.precision == "mixed":
         from pygw_gb300 import eps as peps
-        inp.wb = peps.mixed_omega_batch(inp.nb1, inp.nb2, inp.nkp, w.npb, w.nom)
+        inp.wb = a.omega_batch or peps.mixed_omega_batch(inp.nb1, inp.nb2, inp.nkp, w.npb, w.nom)
+    inp.kb_split = a.kb_split
     # replicas: each rank runs its contiguous block of q points (the reference's mpiSplitArray)
     from pygw_gb300 import replicas
     inp.qs = replicas.my_points(inp.qs, rank, world) or inp.qs[:1]

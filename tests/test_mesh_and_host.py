@@ -90,3 +90,30 @@ def test_capi_library_exports_every_declared_symbol():
     assert l2.pg_bz_calcqdepw_par2_workspace(32, 64, 0, 15, 0, 16, 384, 4) < \
         l2.pg_bz_calcqdepw_par2_workspace(32, 64, 0, 15, 0, 16, 384, 0)
     assert l2.pg_eps_inverse_f64_workspace(0, 4) == 0
+
+
+def test_selfc_entry_points_validate_on_the_host():
+    """The self-energy entry points reject bad sizes, null pointers and short
+    workspaces before any device call, and their size queries are host code."""
+    from pygw_gb300 import _lib
+    lib = _lib.load()
+    EARG, EWORK = -1, -2
+    # workspace queries: zero for bad sizes, growing with the k-points and the frequency batch
+    assert lib.pg_selfc_mwm_workspace(0, 10, 64, 2, 1) == 0
+    assert lib.pg_selfc_mwm_workspace(1, 10, 64, 2, 0) > 0
+    w1 = lib.pg_selfc_mwm_workspace(1, 10, 64, 2, 1)
+    assert lib.pg_selfc_mwm_workspace(2, 10, 64, 2, 1) > w1 < lib.pg_selfc_mwm_workspace(1, 10, 64, 4, 1)
+    assert lib.pg_selfc_convolution_workspace(0, 2, 3, 4, 0, 0) == 0
+    assert lib.pg_selfc_convolution_workspace(1, 2, 3, 4, 8, 0) > lib.pg_selfc_convolution_workspace(1, 2, 3, 4, 0, 0)
+    fake = 0x1000                     # never dereferenced: every call below fails its checks first
+    assert lib.pg_selfc_mwm(None, 1, 10, 64, fake, 2, 0.5, fake, 0, 2, None, 0, None, None) == EARG
+    assert lib.pg_selfc_mwm(fake, 0, 10, 64, fake, 2, 0.5, fake, 0, 2, None, 0, None, None) == EARG
+    assert lib.pg_selfc_mwm(fake, 1, 10, 64, fake, 2, 0.5, fake, 1, 2, None, 0, None, None) == EARG
+    assert lib.pg_selfc_mwm(fake, 1, 10, 64, fake, 2, 0.5, fake, 1, 2, fake, w1 - 1, None, None) == EWORK
+    assert lib.pg_selfc_mwm_q0(fake, 1, 2, 5, 64, -1, 2, fake, fake, fake, 1.0, 1.0, fake, None) == EARG
+    assert lib.pg_selfc_convolution(fake, 1, 2, 3, 4, None, fake, fake, 0, None, None, None, None, 0, fake,
+                                    None) == EARG
+    assert lib.pg_selfc_convolution(fake, 1, 2, 3, 4, fake, fake, fake, 8, fake, fake, fake, fake, 16, fake,
+                                    None) == EWORK
+    assert lib.pg_selfc_convolution_svd(fake, 1, 2, 3, 0, 4, fake, fake, fake, fake, fake, 1 << 20, fake,
+                                        None) == EARG
