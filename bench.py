@@ -296,8 +296,9 @@ def bf16_peak():
 # measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one capture)
 # per launch shape: (workload, N_PB, k-points, frequencies per launch).
 MEASURED_GEMM_TRAFFIC = {
-    ("C3", 1200, 216, 1): 423.06e9 + 0.64e9,
+    ("C3", 1200, 216, 1): 426.53e9 + 0.65e9,
     ("C3", 1200, 216, 2): 1050.0e9 + 1.83e9,
+    ("C3", 1200, 216, 4): 2280.0e9 + 3.79e9,
 }
 
 
