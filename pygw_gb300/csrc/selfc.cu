@@ -276,26 +276,89 @@ __device__ __forceinline__ double2 conv_term(double e, const double2* f, size_t 
   return res;
 }
 
-// sc[k][ie1][iom] = Σ_ie2 conv_term(enk[k][ie2], f[k][·][ie1,ie2], mwm[k][iom][ie1,ie2], ω_iom):
-// all_fr_convolutions with f = mwm on the same mesh; few_fr_convolutions
-// with f = the interpolated mwm on the dense mesh (omd, womd, nd).
-__global__ void k_fr_conv(const double2* __restrict__ mwm, const double2* __restrict__ f, const double* __restrict__ enk,
-                          const double* __restrict__ om, const double* __restrict__ omd,
-                          const double* __restrict__ womd, int nk, int nb1, int nb2, int nom, int nd,
-                          double2* __restrict__ sc) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)nk * nb1 * nom) return;
-  const int iom = (int)(t % nom), ie1 = (int)((t / nom) % nb1), k = (int)(t / ((long long)nom * nb1));
+// sc[k][ie1][iom] = Σ_ie2 of the fr_convolution2 term of f[k][·][ie1,ie2] at
+// enk[k][ie2] and ω_iom, with mwm[k][iom][ie1,ie2] as the value subtracted and
+// in the arctangent term: all_fr_convolutions with f = mwm on the same mesh,
+// few_fr_convolutions with f = the interpolated mwm on the dense mesh
+// (omd, womd, nd).  One block per (k, iom): the weighted inverse denominators
+// womd_i/(ωd_i² + (e − iω)²) and the arctangents depend on (k, ie2, iom) only,
+// so a block computes them once per chunk of 16 ie2 in shared memory and
+// every ie1 row uses them (the per-term complex division was the cost).
+// 256 threads = 16 ie1 × 16 ie2 of the chunk; ie1 beyond 16 in further passes.
+constexpr int CONV_E2 = 16;
+constexpr int CONV_MAXD = 128;      // mesh points held per chunk (larger meshes in slices)
+__global__ void __launch_bounds__(256) k_fr_conv(const double2* __restrict__ mwm, const double2* __restrict__ f,
+                                                 const double* __restrict__ enk, const double* __restrict__ om,
+                                                 const double* __restrict__ omd, const double* __restrict__ womd,
+                                                 int nk, int nb1, int nb2, int nom, int nd,
+                                                 double2* __restrict__ sc) {
+  const double PI_F = 3.14159265358979;         // the truncated π of fnc.f90:71
+  __shared__ double2 D[CONV_E2][CONV_MAXD];     // 32 KB
+  __shared__ double2 AT[CONV_E2];               // atan(ωd_last/(e − iω))/π
+  __shared__ double2 EO[CONV_E2];               // e − iω
+  const int iom = blockIdx.x, k = blockIdx.y;
+  const int tj = threadIdx.x & 15, ti = threadIdx.x >> 4;
   const size_t P = (size_t)nb1 * nb2;
-  double2 sum = make_double2(0.0, 0.0);
-  for (int ie2 = 0; ie2 < nb2; ie2++) {
-    const size_t p = (size_t)ie1 * nb2 + ie2;
-    const double2 fi = mwm[((size_t)k * nom + iom) * P + p];
-    const double2 v = conv_term(enk[(size_t)k * nb2 + ie2], f + (size_t)k * nd * P + p, P, fi, om[iom], omd, womd, nd);
-    sum.x += v.x;
-    sum.y += v.y;
+  const double omi = om[iom];
+  for (int e10 = 0; e10 < nb1; e10 += 16) {
+    const int ie1 = e10 + ti;
+    double2 sum = make_double2(0.0, 0.0);
+    for (int c0 = 0; c0 < nb2; c0 += CONV_E2) {
+      const int ie2 = c0 + tj;
+      const bool live = ie1 < nb1 && ie2 < nb2;
+      const size_t p = (size_t)ie1 * nb2 + ie2;
+      const double2 fi = live ? mwm[((size_t)k * nom + iom) * P + p] : make_double2(0.0, 0.0);
+      double2 s0 = make_double2(0.0, 0.0);
+      for (int i0 = 0; i0 < nd; i0 += CONV_MAXD) {
+        const int ni = min(CONV_MAXD, nd - i0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < CONV_E2 * ni; e += blockDim.x) {
+          const int jj = e / ni, ii = e - jj * ni;
+          const int j2 = c0 + jj, i = i0 + ii;
+          if (j2 < nb2) {
+            const double2 eo = make_double2(enk[(size_t)k * nb2 + j2], -omi);
+            const double2 eo2 = cmul(eo, eo);
+            const double2 one = make_double2(womd[i], 0.0);
+            D[jj][ii] = cdiv(one, make_double2(omd[i] * omd[i] + eo2.x, eo2.y));
+          }
+        }
+        if (i0 == 0 && threadIdx.x < CONV_E2 && c0 + (int)threadIdx.x < nb2) {
+          const double2 eo = make_double2(enk[(size_t)k * nb2 + c0 + threadIdx.x], -omi);
+          EO[threadIdx.x] = eo;
+          const double2 at = catan_(cdiv(make_double2(omd[nd - 1], 0.0), eo));
+          AT[threadIdx.x] = make_double2(at.x / PI_F, at.y / PI_F);
+        }
+        __syncthreads();
+        if (live) {
+          const double2* fr = f + (size_t)k * nd * P + p;
+          for (int ii = 0; ii < ni; ii++) {
+            const double2 v = fr[(size_t)(i0 + ii) * P];
+            const double2 dv = make_double2(v.x - fi.x, v.y - fi.y);
+            const double2 q = cmul(dv, D[tj][ii]);
+            s0.x += q.x;
+            s0.y += q.y;
+          }
+        }
+      }
+      if (live) {
+        const double2 t0 = cmul(EO[tj], s0);
+        double2 res = make_double2(t0.x / PI_F, t0.y / PI_F);
+        if (hypot(fi.x, fi.y) > 1e-16) {
+          const double2 v = cmul(fi, AT[tj]);
+          res.x += v.x;
+          res.y += v.y;
+        }
+        sum.x += res.x;
+        sum.y += res.y;
+      }
+    }
+    // the 16 ie2 lanes of a row are 16 consecutive threads
+    for (int o = 8; o > 0; o >>= 1) {
+      sum.x += __shfl_xor_sync(0xffffffffu, sum.x, o);
+      sum.y += __shfl_xor_sync(0xffffffffu, sum.y, o);
+    }
+    if (tj == 0 && ie1 < nb1) sc[((size_t)k * nb1 + ie1) * nom + iom] = sum;
   }
-  sc[((size_t)k * nb1 + ie1) * nom + iom] = sum;
 }
 
 // iopfreq 4 (mcommon.py:126-140): f[k][j][p] = Σ_i S[j][i]·(ω_i² + 1)·mwm[k][i][p] / (ωd_j² + 1)
@@ -467,12 +530,13 @@ extern "C" int pg_selfc_convolution(const void* mwm, int nk, int nb1, int nb2, i
                                     void* sc, void* stream) {
   if (!mwm || !enk || !omega || !sc || nk <= 0 || nb1 <= 0 || nb2 <= 0 || nom <= 0 || n_dense < 0) return PG_EARG;
   cudaStream_t s = (cudaStream_t)stream;
-  const long long n = (long long)nk * nb1 * nom;
+  if (nk > 65535) return PG_ETOOBIG;
   const double2* m = (const double2*)mwm;
   if (n_dense == 0) {
     if (!womeg) return PG_EARG;
-    k_fr_conv<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(m, m, enk, omega, omega, womeg, nk, nb1, nb2, nom, nom,
-                                                          (double2*)sc);
+    if (nom > 65535) return PG_ETOOBIG;
+    k_fr_conv<<<dim3((unsigned)nom, (unsigned)nk), 256, 0, s>>>(m, m, enk, omega, omega, womeg, nk, nb1, nb2, nom,
+                                                                nom, (double2*)sc);
     pg_count_launches(1);
     return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ECUDA;
   }
@@ -482,8 +546,9 @@ extern "C" int pg_selfc_convolution(const void* mwm, int nk, int nb1, int nb2, i
   const int P = nb1 * nb2;
   const long long ni = (long long)nk * P * n_dense;
   k_interp<<<(unsigned)((ni + 127) / 128), 128, 0, s>>>(m, spline, omega, omega_dense, nk, P, nom, n_dense, f);
-  k_fr_conv<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(m, f, enk, omega, omega_dense, womeg_dense, nk, nb1, nb2, nom,
-                                                        n_dense, (double2*)sc);
+  if (nom > 65535) return PG_ETOOBIG;
+  k_fr_conv<<<dim3((unsigned)nom, (unsigned)nk), 256, 0, s>>>(m, f, enk, omega, omega_dense, womeg_dense, nk, nb1, nb2,
+                                                              nom, n_dense, (double2*)sc);
   pg_count_launches(2);
   return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ECUDA;
 }

@@ -106,7 +106,7 @@ def test_convolution_dense_mesh_matches_oracle():
     om, wom, mwm, enk = _conv_case(22)
     nk, nom, P = mwm.shape
     nb1, nb2 = 3, 7
-    omd = np.geomspace(0.005, 80.0, 41)          # denser, and beyond both ends (extrapolation)
+    omd = np.geomspace(0.005, 80.0, 150)         # denser (two slices of the kernel's 128-point tile), beyond both ends
     womd = np.gradient(omd)
     got = gsc.convolution(torch.from_numpy(mwm).cuda(), enk, om, wom, nb1, nb2, dense=(omd, womd)).cpu().numpy()
     for k in range(nk):
