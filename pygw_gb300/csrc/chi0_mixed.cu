@@ -18,8 +18,10 @@
 // < 2^24) the epilogue warps move the multiples of 2^12 into an FP32 register
 // accumulator (exact while below 2^36 — the host splits K so it stays
 // below 2^35) and leave the remainder in place.  Each group's integer is
-// then combined in FP64.  The only rounding is the dropped 5th-digit
-// residual and the dropped d ≥ 5 pairs (≈ 1e-11 relative per row scale).
+// then combined into the output tile: in FP64 for the symmetric χ0 product,
+// as a float pair (≈ 2^-47 relative) for the general product.  The only other
+// rounding is the dropped 5th-digit residual and the dropped d ≥ 5 pairs
+// (≈ 1e-11 relative per row scale).
 //
 // Kernel layout: a cluster of two CTAs owns a 256×256 block of the upper
 // block triangle of G, per frequency, per K-split.  CTA r of the cluster

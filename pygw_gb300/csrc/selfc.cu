@@ -15,7 +15,8 @@
 //     fused into the tile epilogue;
 //   * split precision: the general digit GEMM with one digit set for
 //     A = [[Re M, Im M], [−Im M, Re M]] shared by the frequencies and B = the
-//     columns [Re W; Im W] per frequency, then k_mwm_reduce in FP64.
+//     columns [Re W; Im W] per frequency (float-pair output tiles), then
+//     k_mwm_reduce in float-pair arithmetic against a float-pair copy of M.
 // Layouts: minm [nk][P][N], W [nom][N][N] (column-major per frequency),
 // mwm [nk][nom][P], enk [nk][nb2], sc [nk][nb1][nom]; all complex128 but enk.
 #include <cuda_runtime.h>
