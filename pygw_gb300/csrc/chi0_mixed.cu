@@ -696,13 +696,18 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   const float bb = s - a;
   e = (a - (s - bb)) + (b - bb);
 }
+// With wnext (the next batch's weights, nwn frequencies) the same pass also
+// forms that batch's row maxima into rmax_next, exactly as k_rowmax_B does
+// (the three-digit |V| it needs is vhi here), so only the first batch of a
+// contraction needs its own k_rowmax_B pass over the A digits.
 __global__ void k_digits_B(const __nv_bfloat16* __restrict__ adig, const int* eA, const float2* __restrict__ wpair,
-                           const int* fB, int R, int R_pad, long long K_pad, int nw, __nv_bfloat16* bdig) {
+                           const int* fB, int R, int R_pad, long long K_pad, int nw, __nv_bfloat16* bdig,
+                           const float2* __restrict__ wnext, int nwn, unsigned* rmax_next) {
   const long long k0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 4;
   const int r = blockIdx.y;
-  if (k0 >= K_pad) return;
-  float vhi[4], vlo[4];
-  {
+  const bool in = k0 < K_pad;
+  float vhi[4] = {0.0f, 0.0f, 0.0f, 0.0f}, vlo[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  if (in) {
     float a[S][4];
 #pragma unroll
     for (int s = 0; s < S; s++) ld_bf16x4(adig + digit_index(s, r, k0, R_pad, (int)(K_pad >> 6)), a[s]);
@@ -712,7 +717,7 @@ __global__ void k_digits_B(const __nv_bfloat16* __restrict__ adig, const int* eA
       vlo[j] = (a[3][j] * 0x1p-32f + a[4][j] * 0x1p-40f);                         // exact
     }
   }
-  for (int wl = 0; wl < nw; wl++) {
+  for (int wl = 0; wl < nw && in; wl++) {
     const float4* wp = reinterpret_cast<const float4*>(wpair + (size_t)wl * K_pad + k0);
     const float4 w01 = wp[0], w23 = wp[1];
     const float wh[4] = {w01.x, w01.z, w23.x, w23.z}, wo[4] = {w01.y, w01.w, w23.y, w23.w};
@@ -739,6 +744,27 @@ __global__ void k_digits_B(const __nv_bfloat16* __restrict__ adig, const int* eA
     }
 #pragma unroll
     for (int s = 0; s < S; s++) st_bf16x4(bdig + digit_index(wl * S + s, r, k0, R_pad, (int)(K_pad >> 6)), dg[s]);
+  }
+  if (wnext == nullptr) return;               // uniform across the block
+  const bool inr = in && r < R;
+  __shared__ float sm[32];
+  for (int wl = 0; wl < nwn; wl++) {
+    float m = 0.0f;
+    if (inr) {
+      const float4* wp = reinterpret_cast<const float4*>(wnext + (size_t)wl * K_pad + k0);
+      const float4 w01 = wp[0], w23 = wp[1];
+      m = fmaxf(fmaxf(__fmul_ru(fabsf(vhi[0]), fabsf(w01.x)), __fmul_ru(fabsf(vhi[1]), fabsf(w01.z))),
+                fmaxf(__fmul_ru(fabsf(vhi[2]), fabsf(w23.x)), __fmul_ru(fabsf(vhi[3]), fabsf(w23.z))));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float mm = sm[0];
+      for (int i = 1; i < (int)(blockDim.x >> 5); i++) mm = fmaxf(mm, sm[i]);
+      if (mm > 0.0f) atomicMax(rmax_next + (size_t)wl * R_pad + r, __float_as_uint(mm));
+    }
+    __syncthreads();
   }
 }
 
@@ -859,8 +885,10 @@ static MixedLayout mixed_layout(int nb1, int nb2, int nkp, int npb, int wb, int 
   L.off_adig = o; o += al256((size_t)S * L.R_pad * L.K_pad * 2);
   L.off_bdig = o; o += al256((size_t)L.wbp * S * L.R_pad * L.K_pad * 2);
   L.off_tmax = o; o += al256((size_t)L.R_pad * L.nkb * 4);
-  L.off_wpair = o; o += al256((size_t)L.wbp * L.K_pad * 8);
-  L.off_rmax = o; o += al256((size_t)L.wbp * L.R_pad * 4);  // row maxima of |V·c·w| (float bits)
+  // two preparation batches' weights and row maxima (the next batch's maxima
+  // are formed while the current batch's digits are written)
+  L.off_wpair = o; o += al256((size_t)2 * L.wbp * L.K_pad * 8);
+  L.off_rmax = o; o += al256((size_t)2 * L.wbp * L.R_pad * 4);  // row maxima of |V·c·w| (float bits)
   L.off_eA = o; o += al256((size_t)L.R_pad * 4);
   L.off_fB = o; o += al256((size_t)L.wbp * L.R_pad * 4);
   L.off_out = o; o += al256((size_t)L.nsplit * wb * L.npair * TM * TM * 8);
@@ -956,18 +984,37 @@ static int chi0_mixed_impl(const void* minm, int nkp, int k0, const int* kstart,
   attr[0].val.clusterDim.z = 1;
   op.wl0 = 0;
   const int wbp = L.wbp;
-  for (int op0 = 0; op0 < nom; op0 += wbp) {
-    // B digits of the frequencies op0 … op0+npw−1: one pass over the A digits
-    const int npw = (op0 + wbp <= nom) ? wbp : nom - op0;
-    k_weights_prep<<<dim3(L.nkb, npw), 64, 0, s>>>(kcw, nb1, nb2, nkp_total, k0, nkp, kstart, knb2, op0, npw, coef,
-                                                   L.K, L.K_pad, wpair);
-    if (cudaMemsetAsync(rmax, 0, (size_t)wbp * L.R_pad * 4, s) != cudaSuccess) return PG_ECUDA;
+  const size_t wstride = (size_t)wbp * L.K_pad, rstride = (size_t)wbp * L.R_pad;
+  // first batch: weights and row maxima by their own pass
+  {
+    const int npw0 = wbp < nom ? wbp : nom;
+    k_weights_prep<<<dim3(L.nkb, npw0), 64, 0, s>>>(kcw, nb1, nb2, nkp_total, k0, nkp, kstart, knb2, 0, npw0, coef,
+                                                    L.K, L.K_pad, wpair);
+    if (cudaMemsetAsync(rmax, 0, rstride * 4, s) != cudaSuccess) return PG_ECUDA;
     k_rowmax_B<<<dim3((unsigned)((L.K_pad + 1023) / 1024), L.R_pad), 256, 0, s>>>(adig, wpair, L.R, L.R_pad, L.K_pad,
-                                                                                  npw, rmax);
-    k_row_exp_B<<<(npw * L.R_pad + 255) / 256, 256, 0, s>>>(rmax, eA, L.R, L.R_pad, npw, fB);
-    k_digits_B<<<dim3((unsigned)((L.K_pad + 1023) / 1024), L.R_pad), 256, 0, s>>>(adig, eA, wpair, fB, L.R, L.R_pad,
-                                                                                  L.K_pad, npw, bdig);
-    pg_count_launches(4);
+                                                                                  npw0, rmax);
+    pg_count_launches(2);
+  }
+  for (int op0 = 0, bi = 0; op0 < nom; op0 += wbp, bi++) {
+    // B digits of the frequencies op0 … op0+npw−1 (one pass over the A digits),
+    // which also forms the next batch's row maxima
+    const int npw = (op0 + wbp <= nom) ? wbp : nom - op0;
+    const int cur = bi & 1, nxt = cur ^ 1;
+    const int on = op0 + wbp, npn = on < nom ? ((on + wbp <= nom) ? wbp : nom - on) : 0;
+    float2* wcur = wpair + cur * wstride;
+    float2* wnxt = wpair + nxt * wstride;
+    unsigned* rcur = rmax + cur * rstride;
+    unsigned* rnxt = rmax + nxt * rstride;
+    k_row_exp_B<<<(npw * L.R_pad + 255) / 256, 256, 0, s>>>(rcur, eA, L.R, L.R_pad, npw, fB);
+    if (npn > 0) {
+      k_weights_prep<<<dim3(L.nkb, npn), 64, 0, s>>>(kcw, nb1, nb2, nkp_total, k0, nkp, kstart, knb2, on, npn, coef,
+                                                     L.K, L.K_pad, wnxt);
+      if (cudaMemsetAsync(rnxt, 0, rstride * 4, s) != cudaSuccess) return PG_ECUDA;
+      pg_count_launches(1);
+    }
+    k_digits_B<<<dim3((unsigned)((L.K_pad + 1023) / 1024), L.R_pad), 256, 0, s>>>(
+        adig, eA, wcur, fB, L.R, L.R_pad, L.K_pad, npw, bdig, npn > 0 ? wnxt : nullptr, npn, rnxt);
+    pg_count_launches(2);
     for (int g0 = 0; g0 < npw; g0 += wb) {
       const int nw = (g0 + wb <= npw) ? wb : npw - g0;
       const int om0 = op0 + g0;
