@@ -553,7 +553,19 @@ __global__ void k_row_exp_A(const float* tmax, int R, int R_pad, int nkb, int* e
   if (threadIdx.x == 0) eA[r] = row_exponent(sm[0]);
 }
 
-// A digits (bf16, K-block major, see digit_index); computed exactly in FP64.
+// Knuth's two-sum: s = fl(a + b), e = the exact rounding error (s + e = a + b).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// A digits (bf16, K-block major, see digit_index).  The value scaled by 2^-eA
+// is split once into a float pair (hi = nearest float, lo = nearest float to
+// the rest, ≈ 48 bits), and the digits are taken from the pair in FP32 with
+// exact two-sums, as k_digits_B does: |value − digits| stays below 2^(eA−40),
+// and FP64 work drops from ≈ 17 operations per value to 4 (GB300 runs FP64
+// at a small fraction of the FP32 rate).
 __global__ void k_digits_A(const double2* __restrict__ minm, long long K, int N, int R_pad, long long K_pad,
                            const int* eA, __nv_bfloat16* adig) {
   __shared__ double2 tile[32][33];
@@ -572,12 +584,14 @@ __global__ void k_digits_A(const double2* __restrict__ minm, long long K, int N,
     const double2 m = tile[tx][j];
     for (int part = 0; part < 2; part++) {
       const int r = part ? N + I : I;
-      double y = ldexp(part ? m.y : m.x, -eA[r]);
+      const double y = ldexp(part ? m.y : m.x, -eA[r]);
+      const float h = __double2float_rn(y);
+      float yh = h, yl = __double2float_rn(y - (double)h);
       for (int s = 0; s < S; s++) {
-        const double t = y * 256.0;
-        const double dg = rint(t);
-        y = t - dg;
-        adig[digit_index(s, r, k, R_pad, (int)(K_pad >> 6))] = __float2bfloat16_rn((float)dg);
+        const float t = yh * 256.0f;        // exact
+        const float d = rintf(t);
+        two_sum(t - d, yl * 256.0f, yh, yl);   // t − d and yl·256 are exact
+        adig[digit_index(s, r, k, R_pad, (int)(K_pad >> 6))] = __float2bfloat16_rn(d);
       }
     }
   }
@@ -691,11 +705,6 @@ __global__ void k_row_exp_B(const unsigned* rmax, const int* eA, int R, int R_pa
 // V = 2^eA (hi + lo) exactly (hi: digits 0-2, lo: digits 3-4), c·w = wh + wl,
 // product to ~46 bits with one exact FMA error term, then 5 signed digits
 // relative to 2^fB carried as an unevaluated float pair.
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
 // With wnext (the next batch's weights, nwn frequencies) the same pass also
 // forms that batch's row maxima into rmax_next, exactly as k_rowmax_B does
 // (the three-digit |V| it needs is vhi here), so only the first batch of a
