@@ -560,6 +560,22 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bb)) + (b - bb);
 }
 
+// One digit step of a float pair (yh, yl) with |yl| ≤ ulp(yh)/2: d = the
+// nearest integer to 256·yh, and (yh, yl) ← the pair of 256·(yh + yl) − d.
+// r = 256·yh − d is exact and a multiple of u = ulp(256·yh) (u ≤ 1 whenever
+// 256·yh is not an integer; r = 0 otherwise), while |256·yl| ≤ u/2, so r = 0
+// or |r| ≥ |256·yl|: Dekker's fast two-sum is then exact and gives the same
+// pair as the two-sum above in half the operations, with |yl| ≤ ulp(yh)/2 again.
+__device__ __forceinline__ float digit_step(float& yh, float& yl) {
+  const float t = yh * 256.0f;        // exact
+  const float d = rintf(t);
+  const float r = t - d;              // exact
+  const float b = yl * 256.0f;        // exact
+  yh = r + b;
+  yl = b - (yh - r);
+  return d;
+}
+
 // A digits (bf16, K-block major, see digit_index).  The value scaled by 2^-eA
 // is split once into a float pair (hi = nearest float, lo = nearest float to
 // the rest, ≈ 48 bits), and the digits are taken from the pair in FP32 with
@@ -588,9 +604,7 @@ __global__ void k_digits_A(const double2* __restrict__ minm, long long K, int N,
       const float h = __double2float_rn(y);
       float yh = h, yl = __double2float_rn(y - (double)h);
       for (int s = 0; s < S; s++) {
-        const float t = yh * 256.0f;        // exact
-        const float d = rintf(t);
-        two_sum(t - d, yl * 256.0f, yh, yl);   // t − d and yl·256 are exact
+        const float d = digit_step(yh, yl);
         adig[digit_index(s, r, k, R_pad, (int)(K_pad >> 6))] = __float2bfloat16_rn(d);
       }
     }
@@ -743,13 +757,7 @@ __global__ void k_digits_B(const __nv_bfloat16* __restrict__ adig, const int* eA
       float yh = fast ? ph * p2 : ldexpf(ph, sh), yl = fast ? pl * p2 : ldexpf(pl, sh);
       two_sum(yh, yl, yh, yl);
 #pragma unroll
-      for (int s = 0; s < S; s++) {
-        const float t = yh * 256.0f;
-        const float d = rintf(t);
-        const float rh = t - d;              // exact
-        two_sum(rh, yl * 256.0f, yh, yl);
-        dg[s][j] = d;
-      }
+      for (int s = 0; s < S; s++) dg[s][j] = digit_step(yh, yl);
     }
 #pragma unroll
     for (int s = 0; s < S; s++) st_bf16x4(bdig + digit_index(wl * S + s, r, k0, R_pad, (int)(K_pad >> 6)), dg[s]);
