@@ -723,9 +723,10 @@ __global__ void k_row_exp_B(const unsigned* rmax, const int* eA, int R, int R_pa
 // forms that batch's row maxima into rmax_next, exactly as k_rowmax_B does
 // (the three-digit |V| it needs is vhi here), so only the first batch of a
 // contraction needs its own k_rowmax_B pass over the A digits.
-__global__ void k_digits_B(const __nv_bfloat16* __restrict__ adig, const int* eA, const float2* __restrict__ wpair,
-                           const int* fB, int R, int R_pad, long long K_pad, int nw, __nv_bfloat16* bdig,
-                           const float2* __restrict__ wnext, int nwn, unsigned* rmax_next) {
+__global__ void __launch_bounds__(256, 8) k_digits_B(const __nv_bfloat16* __restrict__ adig, const int* eA,
+                                                     const float2* __restrict__ wpair, const int* fB, int R, int R_pad,
+                                                     long long K_pad, int nw, __nv_bfloat16* bdig,
+                                                     const float2* __restrict__ wnext, int nwn, unsigned* rmax_next) {
   const long long k0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 4;
   const int r = blockIdx.y;
   const bool in = k0 < K_pad;

@@ -145,7 +145,10 @@ __global__ void __launch_bounds__(512) k_gj32_panel(float2* X, int N, int c0, in
 
 // Rank-b update of the non-panel columns: A[i,c] ← (i in panel ? 0 : A[i,c]) + Σ_j W[i,j]·S[j,c],
 // S[j,c] = A[c0+j, c] read before any write of column c.  Block: 32 columns
-// (panel columns skipped) × all rows of one ω; grid (ceil(N/32), nw).
+// (panel columns skipped) × all rows of one ω; grid (ceil(N/32), nw).  Each
+// thread loads eight columns of its row before it updates them, so eight
+// loads per warp are in flight (one at a time left the kernel bound by
+// DRAM latency, at about a fifth of the copy bandwidth).
 constexpr int GJ_BMAX = 16;
 __global__ void __launch_bounds__(256) k_gj32_update(float2* X, int N, int c0, int b) {
   __shared__ float2 Ss[GJ_BMAX][32];
@@ -162,20 +165,29 @@ __global__ void __launch_bounds__(256) k_gj32_update(float2* X, int N, int c0, i
 #pragma unroll
     for (int j = 0; j < GJ_BMAX; j++) wr[j] = (j < b) ? E[(size_t)i + (size_t)N * (c0 + j)] : make_float2(0.0f, 0.0f);
     const bool prow = i >= c0 && i < c0 + b;
-    for (int cc = 0; cc < 32; cc++) {
-      const int c = cbase + cc;
-      if (c >= N) break;
-      if (c >= c0 && c < c0 + b) continue;
-      float2 acc = prow ? make_float2(0.0f, 0.0f) : E[(size_t)i + (size_t)N * c];
+    for (int c8 = 0; c8 < 32; c8 += 8) {
+      float2 acc[8];
+      bool upd[8];
 #pragma unroll
-      for (int j = 0; j < GJ_BMAX; j++) {
-        if (j < b) {
-          const float2 sj = Ss[j][cc];
-          acc.x += wr[j].x * sj.x - wr[j].y * sj.y;
-          acc.y += wr[j].x * sj.y + wr[j].y * sj.x;
+      for (int q = 0; q < 8; q++) {
+        const int c = cbase + c8 + q;
+        upd[q] = c < N && (c < c0 || c >= c0 + b);
+        acc[q] = (upd[q] && !prow) ? E[(size_t)i + (size_t)N * c] : make_float2(0.0f, 0.0f);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+#pragma unroll
+        for (int j = 0; j < GJ_BMAX; j++) {
+          if (j < b) {
+            const float2 sj = Ss[j][c8 + q];
+            acc[q].x += wr[j].x * sj.x - wr[j].y * sj.y;
+            acc[q].y += wr[j].x * sj.y + wr[j].y * sj.x;
+          }
         }
       }
-      E[(size_t)i + (size_t)N * c] = acc;
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        if (upd[q]) E[(size_t)i + (size_t)N * (cbase + c8 + q)] = acc[q];
     }
   }
 }
@@ -297,7 +309,8 @@ __global__ void k_residual(const double* __restrict__ out, const int* eA, const 
 }
 
 // Xnew = X + X·R (complex, FP32 products and accumulation, FP64 sum with X).
-// 64×64 output tile per block, 16×16 threads with 4×4 outputs each.
+// 64×64 output tile per block, 16×16 threads with 4×4 outputs each; the next
+// 16-wide K slice is loaded into registers while the current one is used.
 template <typename T>
 __global__ void __launch_bounds__(256) k_correct(const T* __restrict__ X, const double2* __restrict__ R, int N,
                                                  double2* __restrict__ Xnew) {
@@ -313,18 +326,29 @@ __global__ void __launch_bounds__(256) k_correct(const T* __restrict__ X, const 
   for (int a = 0; a < 4; a++)
 #pragma unroll
     for (int b = 0; b < 4; b++) acc[a][b] = make_float2(0.0f, 0.0f);
-  for (int k0 = 0; k0 < N; k0 += 16) {
-    for (int e = threadIdx.x; e < 1024; e += 256) {
+  double2 vx[4], vr[4];                                   // this thread's loads of one K slice
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int e = threadIdx.x + 256 * q;
       const int ii = e & 63, kk = e >> 6;                 // X(i0+ii, k0+kk): 64 consecutive rows
       const int i = i0 + ii, k = k0 + kk;
-      const double2 v = (i < N && k < N) ? ld2(Xw + (size_t)N * k + i) : make_double2(0.0, 0.0);
-      sx[kk][ii] = make_float2((float)v.x, (float)v.y);
+      vx[q] = (i < N && k < N) ? ld2(Xw + (size_t)N * k + i) : make_double2(0.0, 0.0);
       const int kr = e & 15, jj = e >> 4;                 // R(k0+kr, j0+jj): 16 consecutive rows
       const int k2 = k0 + kr, j = j0 + jj;
-      const double2 u = (k2 < N && j < N) ? Rw[(size_t)N * j + k2] : make_double2(0.0, 0.0);
-      sr[kr][jj] = make_float2((float)u.x, (float)u.y);
+      vr[q] = (k2 < N && j < N) ? Rw[(size_t)N * j + k2] : make_double2(0.0, 0.0);
+    }
+  };
+  load(0);
+  for (int k0 = 0; k0 < N; k0 += 16) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int e = threadIdx.x + 256 * q;
+      sx[e >> 6][e & 63] = make_float2((float)vx[q].x, (float)vx[q].y);
+      sr[e & 15][e >> 4] = make_float2((float)vr[q].x, (float)vr[q].y);
     }
     __syncthreads();
+    if (k0 + 16 < N) load(k0 + 16);
 #pragma unroll
     for (int kk = 0; kk < 16; kk++) {
       float2 xa[4], rb[4];
