@@ -723,66 +723,77 @@ __global__ void k_row_exp_B(const unsigned* rmax, const int* eA, int R, int R_pa
 // forms that batch's row maxima into rmax_next, exactly as k_rowmax_B does
 // (the three-digit |V| it needs is vhi here), so only the first batch of a
 // contraction needs its own k_rowmax_B pass over the A digits.
-__global__ void __launch_bounds__(256, 8) k_digits_B(const __nv_bfloat16* __restrict__ adig, const int* eA,
+// Block: DB_ROWS rows × 16 threads (4 values each: one 64-value K-block row,
+// 128 bytes), over DB_KB consecutive K-blocks; in the K-block-major digit
+// layout the block's rows of one K-block are DB_ROWS·128 contiguous bytes of
+// every plane (one row per block scattered its accesses in 128-byte pieces
+// R_pad·128 bytes apart).  Dynamic shared memory: nwn·DB_ROWS floats.
+constexpr int DB_ROWS = 16, DB_KB = 8;
+__global__ void __launch_bounds__(256, 6) k_digits_B(const __nv_bfloat16* __restrict__ adig, const int* eA,
                                                      const float2* __restrict__ wpair, const int* fB, int R, int R_pad,
                                                      long long K_pad, int nw, __nv_bfloat16* bdig,
                                                      const float2* __restrict__ wnext, int nwn, unsigned* rmax_next) {
-  const long long k0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 4;
-  const int r = blockIdx.y;
-  const bool in = k0 < K_pad;
-  float vhi[4] = {0.0f, 0.0f, 0.0f, 0.0f}, vlo[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-  if (in) {
-    float a[S][4];
+  extern __shared__ float smax[];                // [nwn][DB_ROWS] row maxima of the next batch
+  const int nkb = (int)(K_pad >> 6);
+  const int lr = threadIdx.x >> 4, lk = threadIdx.x & 15;
+  const int r = blockIdx.y * DB_ROWS + lr;       // < R_pad (a multiple of 256)
+  const int eAr = (r < R) ? eA[r] : 0;
+  for (int i = threadIdx.x; i < nwn * DB_ROWS; i += blockDim.x) smax[i] = 0.0f;
+  __syncthreads();
+  for (int kbi = 0; kbi < DB_KB; kbi++) {
+    const int kb = blockIdx.x * DB_KB + kbi;
+    if (kb >= nkb) break;                        // uniform across the block
+    const long long k0 = (long long)kb * KB + lk * 4;
+    float vhi[4], vlo[4];
+    {
+      float a[S][4];
 #pragma unroll
-    for (int s = 0; s < S; s++) ld_bf16x4(adig + digit_index(s, r, k0, R_pad, (int)(K_pad >> 6)), a[s]);
+      for (int s = 0; s < S; s++) ld_bf16x4(adig + digit_index(s, r, k0, R_pad, nkb), a[s]);
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-      vhi[j] = ((a[0][j] * 0x1p-8f + a[1][j] * 0x1p-16f) + a[2][j] * 0x1p-24f);   // exact
-      vlo[j] = (a[3][j] * 0x1p-32f + a[4][j] * 0x1p-40f);                         // exact
+      for (int j = 0; j < 4; j++) {
+        vhi[j] = ((a[0][j] * 0x1p-8f + a[1][j] * 0x1p-16f) + a[2][j] * 0x1p-24f);   // exact
+        vlo[j] = (a[3][j] * 0x1p-32f + a[4][j] * 0x1p-40f);                         // exact
+      }
     }
-  }
-  for (int wl = 0; wl < nw && in; wl++) {
-    const float4* wp = reinterpret_cast<const float4*>(wpair + (size_t)wl * K_pad + k0);
-    const float4 w01 = wp[0], w23 = wp[1];
-    const float wh[4] = {w01.x, w01.z, w23.x, w23.z}, wo[4] = {w01.y, w01.w, w23.y, w23.w};
-    const int sh = (r < R) ? (eA[r] - fB[(size_t)wl * R_pad + r]) : 0;
-    // 2^sh as a float when it is a normal number (a multiply then scales exactly as ldexpf does)
-    const bool fast = sh >= -126 && sh <= 127;
-    const float p2 = fast ? __int_as_float((sh + 127) << 23) : 1.0f;
-    float dg[S][4];
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const float ph = vhi[j] * wh[j];
-      const float pe = fmaf(vhi[j], wh[j], -ph);
-      const float pl = pe + (vhi[j] * wo[j] + vlo[j] * wh[j]);
-      float yh = fast ? ph * p2 : ldexpf(ph, sh), yl = fast ? pl * p2 : ldexpf(pl, sh);
-      two_sum(yh, yl, yh, yl);
-#pragma unroll
-      for (int s = 0; s < S; s++) dg[s][j] = digit_step(yh, yl);
-    }
-#pragma unroll
-    for (int s = 0; s < S; s++) st_bf16x4(bdig + digit_index(wl * S + s, r, k0, R_pad, (int)(K_pad >> 6)), dg[s]);
-  }
-  if (wnext == nullptr) return;               // uniform across the block
-  const bool inr = in && r < R;
-  __shared__ float sm[32];
-  for (int wl = 0; wl < nwn; wl++) {
-    float m = 0.0f;
-    if (inr) {
-      const float4* wp = reinterpret_cast<const float4*>(wnext + (size_t)wl * K_pad + k0);
+    for (int wl = 0; wl < nw; wl++) {
+      const float4* wp = reinterpret_cast<const float4*>(wpair + (size_t)wl * K_pad + k0);
       const float4 w01 = wp[0], w23 = wp[1];
-      m = fmaxf(fmaxf(__fmul_ru(fabsf(vhi[0]), fabsf(w01.x)), __fmul_ru(fabsf(vhi[1]), fabsf(w01.z))),
-                fmaxf(__fmul_ru(fabsf(vhi[2]), fabsf(w23.x)), __fmul_ru(fabsf(vhi[3]), fabsf(w23.z))));
+      const float wh[4] = {w01.x, w01.z, w23.x, w23.z}, wo[4] = {w01.y, w01.w, w23.y, w23.w};
+      const int sh = (r < R) ? (eAr - fB[(size_t)wl * R_pad + r]) : 0;
+      // 2^sh as a float when it is a normal number (a multiply then scales exactly as ldexpf does)
+      const bool fast = sh >= -126 && sh <= 127;
+      const float p2 = fast ? __int_as_float((sh + 127) << 23) : 1.0f;
+      float dg[S][4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const float ph = vhi[j] * wh[j];
+        const float pe = fmaf(vhi[j], wh[j], -ph);
+        const float pl = pe + (vhi[j] * wo[j] + vlo[j] * wh[j]);
+        float yh = fast ? ph * p2 : ldexpf(ph, sh), yl = fast ? pl * p2 : ldexpf(pl, sh);
+        two_sum(yh, yl, yh, yl);
+#pragma unroll
+        for (int s = 0; s < S; s++) dg[s][j] = digit_step(yh, yl);
+      }
+#pragma unroll
+      for (int s = 0; s < S; s++) st_bf16x4(bdig + digit_index(wl * S + s, r, k0, R_pad, nkb), dg[s]);
     }
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      float mm = sm[0];
-      for (int i = 1; i < (int)(blockDim.x >> 5); i++) mm = fmaxf(mm, sm[i]);
-      if (mm > 0.0f) atomicMax(rmax_next + (size_t)wl * R_pad + r, __float_as_uint(mm));
+    for (int wl = 0; wl < nwn; wl++) {
+      float m = 0.0f;
+      if (r < R) {
+        const float4* wp = reinterpret_cast<const float4*>(wnext + (size_t)wl * K_pad + k0);
+        const float4 w01 = wp[0], w23 = wp[1];
+        m = fmaxf(fmaxf(__fmul_ru(fabsf(vhi[0]), fabsf(w01.x)), __fmul_ru(fabsf(vhi[1]), fabsf(w01.z))),
+                  fmaxf(__fmul_ru(fabsf(vhi[2]), fabsf(w23.x)), __fmul_ru(fabsf(vhi[3]), fabsf(w23.z))));
+      }
+      // maximum over the 16 threads of this row (one half of the warp)
+      for (int o = 8; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+      if (lk == 0) smax[wl * DB_ROWS + lr] = fmaxf(smax[wl * DB_ROWS + lr], m);
     }
-    __syncthreads();
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nwn * DB_ROWS; i += blockDim.x) {
+    const int rr = blockIdx.y * DB_ROWS + (i % DB_ROWS);
+    if (rr < R && smax[i] > 0.0f) atomicMax(rmax_next + (size_t)(i / DB_ROWS) * R_pad + rr, __float_as_uint(smax[i]));
   }
 }
 
@@ -1030,7 +1041,8 @@ static int chi0_mixed_impl(const void* minm, int nkp, int k0, const int* kstart,
       if (cudaMemsetAsync(rnxt, 0, rstride * 4, s) != cudaSuccess) return PG_ECUDA;
       pg_count_launches(1);
     }
-    k_digits_B<<<dim3((unsigned)((L.K_pad + 1023) / 1024), L.R_pad), 256, 0, s>>>(
+    k_digits_B<<<dim3((unsigned)((L.nkb + DB_KB - 1) / DB_KB), L.R_pad / DB_ROWS), 256,
+                 (size_t)(npn > 0 ? npn : 1) * DB_ROWS * sizeof(float), s>>>(
         adig, eA, wcur, fB, L.R, L.R_pad, L.K_pad, npw, bdig, npn > 0 ? wnxt : nullptr, npn, rnxt);
     pg_count_launches(2);
     for (int g0 = 0; g0 < npw; g0 += wb) {
