@@ -600,7 +600,11 @@ __global__ void k_digits_A(const double2* __restrict__ minm, long long K, int N,
     const double2 m = tile[tx][j];
     for (int part = 0; part < 2; part++) {
       const int r = part ? N + I : I;
-      const double y = ldexp(part ? m.y : m.x, -eA[r]);
+      // ·2^-e as a multiply by the normal double 2^-e: the same correctly
+      // rounded product as ldexp (which costs several FP64 operations)
+      const int e = eA[r];
+      const double x = part ? m.y : m.x;
+      const double y = (e >= -1022 && e <= 1022) ? x * __longlong_as_double((long long)(1023 - e) << 52) : ldexp(x, -e);
       const float h = __double2float_rn(y);
       float yh = h, yl = __double2float_rn(y - (double)h);
       for (int s = 0; s < S; s++) {
