@@ -560,19 +560,22 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bb)) + (b - bb);
 }
 
-// One digit step of a float pair (yh, yl) with |yl| ≤ ulp(yh)/2: d = the
-// nearest integer to 256·yh, and (yh, yl) ← the pair of 256·(yh + yl) − d.
-// r = 256·yh − d is exact and a multiple of u = ulp(256·yh) (u ≤ 1 whenever
-// 256·yh is not an integer; r = 0 otherwise), while |256·yl| ≤ u/2, so r = 0
-// or |r| ≥ |256·yl|: Dekker's fast two-sum is then exact and gives the same
-// pair as the two-sum above in half the operations, with |yl| ≤ ulp(yh)/2 again.
-__device__ __forceinline__ float digit_step(float& yh, float& yl) {
-  const float t = yh * 256.0f;        // exact
-  const float d = rintf(t);
-  const float r = t - d;              // exact
-  const float b = yl * 256.0f;        // exact
-  yh = r + b;
-  yl = b - (yh - r);
+// One digit step of a float pair carried scaled by 256, (Yh, Yl) = 256·(yh, yl)
+// with |Yl| ≤ ulp(Yh)/2: d = the nearest integer to Yh, and (Yh, Yl) ← 256 ×
+// the pair of (Yh − d) + Yl.  r = Yh − d is exact and a multiple of u = ulp(Yh)
+// (u ≤ 1 whenever Yh is not an integer; r = 0 otherwise), while |Yl| ≤ u/2, so
+// r = 0 or |r| ≥ |Yl|: Dekker's fast two-sum is then exact.  Its sum and error
+// are formed already scaled by 256 (256·r is exact, so fma(r, 256, ·) rounds
+// once, as the unscaled sum does), six operations per digit; |Yl| ≤ ulp(Yh)/2
+// holds again.  The digits are those of the unscaled two-sum step: scaling by
+// 256 commutes with rounding wherever a digit can be nonzero.
+__device__ __forceinline__ float digit_step(float& Yh, float& Yl) {
+  const float d = rintf(Yh);
+  const float r = Yh - d;               // exact
+  const float B = Yl * 256.0f;          // exact
+  const float S = fmaf(r, 256.0f, B);   // 256·fl(r + Yl)
+  Yl = B + fmaf(r, 256.0f, -S);         // 256 × the exact rounding error of fl(r + Yl)
+  Yh = S;
   return d;
 }
 
@@ -600,11 +603,13 @@ __global__ void k_digits_A(const double2* __restrict__ minm, long long K, int N,
     const double2 m = tile[tx][j];
     for (int part = 0; part < 2; part++) {
       const int r = part ? N + I : I;
-      // ·2^-e as a multiply by the normal double 2^-e: the same correctly
-      // rounded product as ldexp (which costs several FP64 operations)
+      // ·2^(8−e) (the row scaling and the first digit's 256) as a multiply by
+      // a normal double: the same correctly rounded product as ldexp (which
+      // costs several FP64 operations)
       const int e = eA[r];
       const double x = part ? m.y : m.x;
-      const double y = (e >= -1022 && e <= 1022) ? x * __longlong_as_double((long long)(1023 - e) << 52) : ldexp(x, -e);
+      const double y = (e >= -1014 && e <= 1030) ? x * __longlong_as_double((long long)(1031 - e) << 52)
+                                                 : ldexp(x, 8 - e);
       const float h = __double2float_rn(y);
       float yh = h, yl = __double2float_rn(y - (double)h);
       for (int s = 0; s < S; s++) {
@@ -764,16 +769,17 @@ __global__ void __launch_bounds__(256, 6) k_digits_B(const __nv_bfloat16* __rest
       const float4 w01 = wp[0], w23 = wp[1];
       const float wh[4] = {w01.x, w01.z, w23.x, w23.z}, wo[4] = {w01.y, w01.w, w23.y, w23.w};
       const int sh = (r < R) ? (eAr - fB[(size_t)wl * R_pad + r]) : 0;
-      // 2^sh as a float when it is a normal number (a multiply then scales exactly as ldexpf does)
-      const bool fast = sh >= -126 && sh <= 127;
-      const float p2 = fast ? __int_as_float((sh + 127) << 23) : 1.0f;
+      // 2^(sh+8) (the scaling to 2^fB and the first digit's 256) as a float
+      // when it is a normal number (a multiply then scales exactly as ldexpf does)
+      const bool fast = sh >= -134 && sh <= 119;
+      const float p2 = fast ? __int_as_float((sh + 135) << 23) : 1.0f;
       float dg[S][4];
 #pragma unroll
       for (int j = 0; j < 4; j++) {
         const float ph = vhi[j] * wh[j];
         const float pe = fmaf(vhi[j], wh[j], -ph);
         const float pl = pe + (vhi[j] * wo[j] + vlo[j] * wh[j]);
-        float yh = fast ? ph * p2 : ldexpf(ph, sh), yl = fast ? pl * p2 : ldexpf(pl, sh);
+        float yh = fast ? ph * p2 : ldexpf(ph, sh + 8), yl = fast ? pl * p2 : ldexpf(pl, sh + 8);
         two_sum(yh, yl, yh, yl);
 #pragma unroll
         for (int s = 0; s < S; s++) dg[s][j] = digit_step(yh, yl);
