@@ -117,3 +117,37 @@ def test_selfc_entry_points_validate_on_the_host():
                                     None) == EWORK
     assert lib.pg_selfc_convolution_svd(fake, 1, 2, 3, 0, 4, fake, fake, fake, fake, fake, 1 << 20, fake,
                                         None) == EARG
+
+
+@pytest.mark.parametrize("nb1,nb2,nkp,npb,wb,kb_split", [
+    (9, 24, 64, 128, 2, 0),          # C1-sized
+    (23, 192, 216, 1200, 1, 0),      # C3, one frequency per launch
+    (23, 192, 216, 1200, 4, 1000),   # C3, K range per split capped
+    (39, 368, 57, 2000, 1, 0),       # a C5 k-chunk
+    (40, 360, 1000, 2000, 1, 0),     # C5 in one pass: K = 14.4 M
+    (5, 7, 3, 100, 3, 100),          # tiny, padding everywhere
+])
+def test_mixed_layout_keeps_group_sums_exact(nb1, nb2, nkp, npb, wb, kb_split):
+    """The split-precision χ0 layout is host code: every K split is short enough
+    for exact digit-group sums (5 pairs · kb·64 · 129² < 2^35), the splits cover
+    the K-blocks with none empty, the rows pad to whole 256-column blocks, and
+    the workspace regions are 256-byte aligned, in order and large enough."""
+    from pygw_gb300 import _lib
+    lib = _lib.load()
+    offs = (ctypes.c_size_t * 9)()
+    dims = (ctypes.c_longlong * 9)()
+    assert lib.pg_chi0_mixed_layout(nb1, nb2, nkp, npb, wb, kb_split, offs, dims) == 0
+    K, K_pad, R, R_pad, nT, npair, nkb, nsplit, kbs = list(dims)
+    assert K == nb1 * nb2 * nkp and K_pad % 64 == 0 and K <= K_pad < K + 64 and nkb == K_pad // 64
+    assert R == 2 * npb and R_pad % 256 == 0 and R <= R_pad < R + 256
+    assert nT == R_pad // 128 and npair == nT * (nT + 1) // 2
+    assert 5 * kbs * 64 * 129 ** 2 < 2 ** 35
+    if kb_split:
+        assert kbs <= kb_split
+    assert (nsplit - 1) * kbs < nkb <= nsplit * kbs
+    o = list(offs)
+    assert all(x % 256 == 0 for x in o[:8]) and o == sorted(o)
+    assert o[1] - o[0] >= 5 * R_pad * K_pad * 2                      # A digit planes
+    assert o[2] - o[1] >= max(2, wb) * 5 * R_pad * K_pad * 2         # B digit planes
+    assert o[8] - o[7] >= nsplit * wb * npair * 128 * 128 * 8        # group-sum tiles
+    assert lib.pg_chi0_mixed_workspace(nb1, nb2, nkp, npb, wb, kb_split) == o[8]
