@@ -218,7 +218,7 @@ def mixed_omega_batch(nb1, nb2, nkp, npb, nom, budget_bytes=None):
     the digit GEMM two waves of 2-CTA clusters, within a memory budget
     (default: 40 % of the free device memory).  Fewer frequencies per launch
     leave more of L2 to the digit planes they share: at N_PB 1200 and 6³ k one
-    frequency per launch reads 423 GB from DRAM per frequency, two 525 GB, four
+    frequency per launch reads 427 GB from DRAM per frequency, two 525 GB, four
     567 GB, and runs 7 % faster than two."""
     lib = _lib.load()
     if budget_bytes is None:
