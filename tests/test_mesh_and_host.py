@@ -151,3 +151,48 @@ def test_mixed_layout_keeps_group_sums_exact(nb1, nb2, nkp, npb, wb, kb_split):
     assert o[2] - o[1] >= max(2, wb) * 5 * R_pad * K_pad * 2         # B digit planes
     assert o[8] - o[7] >= nsplit * wb * npair * 128 * 128 * 8        # group-sum tiles
     assert lib.pg_chi0_mixed_workspace(nb1, nb2, nkp, npb, wb, kb_split) == o[8]
+
+
+def test_polarization_entry_points_validate_on_the_host():
+    """The weights, χ0 and ε⁻¹ entry points reject null pointers, inconsistent
+    sizes and short workspaces before any device call (host code: runs without
+    a GPU); their workspace queries return 0 for empty problems."""
+    from pygw_gb300 import _lib
+    lib = _lib.load()
+    EARG, EWORK = -1, -2
+    fake = 0x1000                     # never dereferenced: every call below fails its checks first
+    big = 1 << 40
+    # weights: nbnd 10, nkp 8, ncg 0, nomx 3, numin 2 (nb1 4, nb2 8), nom 4, ntet 48
+    assert lib.pg_bz_calcqdepw_par2_workspace(10, 8, 0, 3, 10, 4, 48, 0) == 0          # nb2 = 0
+    ww = lib.pg_bz_calcqdepw_par2_workspace(10, 8, 0, 3, 2, 4, 48, 0)
+    assert ww > 0
+    w8 = (None, 10, 8, 0.0, fake, 0, 3, 2, fake, 4, fake, 48, fake, fake, big, 0, None, None, None)
+    assert lib.pg_bz_calcqdepw_par2(*w8) == EARG                                          # enk null
+    assert lib.pg_bz_calcqdepw_par2(fake, *w8[1:11], 47, *w8[12:]) == EARG                # ntet != 6·nkp
+    assert lib.pg_bz_calcqdepw_par2(fake, *w8[1:7], 10, *w8[8:]) == EARG                  # empty window
+    assert lib.pg_bz_calcqdepw_par2(fake, *w8[1:14], ww - 1, *w8[15:]) == EWORK
+    # FP64 χ0: k0 + nk beyond nkp, wings without their output
+    c8 = (fake, 4, 0, fake, 3, 5, 5, 2, 16, -2.0, fake, None, None, None)
+    assert lib.pg_chi0_accumulate_f64(None, *c8[1:]) == EARG
+    assert lib.pg_chi0_accumulate_f64(fake, 4, 2, *c8[3:]) == EARG
+    assert lib.pg_chi0_accumulate_f64(*c8[:11], fake, None, None) == EARG
+    # split-precision χ0 (kb_split > 0: the layout needs no device query)
+    assert lib.pg_chi0_mixed_workspace(3, 5, 0, 16, 2, 100) == 0
+    wm = lib.pg_chi0_mixed_workspace(3, 5, 5, 16, 2, 100)
+    m8 = (fake, 5, fake, 3, 5, 4, 16, -2.0, fake, fake, big, 2, 100, None, None, None)
+    assert lib.pg_chi0_mixed(None, *m8[1:]) == EARG
+    assert lib.pg_chi0_mixed(*m8[:11], 0, *m8[12:]) == EARG                               # omega_batch 0
+    assert lib.pg_chi0_mixed(*m8[:10], wm - 1, *m8[11:]) == EWORK
+    a8 = (fake, 2, 0, None, None, 0, fake, 3, 5, 5, 4, 16, -2.0, fake, 0, fake, big, 2, 100, None, None, None)
+    assert lib.pg_chi0_mixed_accumulate(*a8[:2], 4, *a8[3:]) == EARG                      # k0 + nk > nkp
+    assert lib.pg_chi0_mixed_accumulate(*a8[:3], fake, None, 20, *a8[6:]) == EARG          # kstart without knb2
+    assert lib.pg_chi0_mixed_accumulate(*a8[:3], fake, fake, 31, *a8[6:]) == EARG          # nK > nk·nb1·nb2
+    # ε⁻¹: q = 0 borders come together; refinement steps 0…2; workspace sizes
+    assert lib.pg_eps_inverse_f64_workspace(0, 4) == 0 and lib.pg_eps_inverse_mixed_workspace(16, 0, 0) == 0
+    wf = lib.pg_eps_inverse_f64_workspace(16, 4)
+    assert lib.pg_eps_inverse_f64(fake, 16, 4, fake, None, fake, fake, big, None) == EARG
+    assert lib.pg_eps_inverse_f64(fake, 16, 4, None, None, None, fake, wf - 1, None) == EWORK
+    wx = lib.pg_eps_inverse_mixed_workspace(16, 4, 0)
+    assert lib.pg_eps_inverse_mixed(fake, 16, 4, None, None, None, fake, big, 0, 3, None, None) == EARG
+    assert lib.pg_eps_inverse_mixed(fake, 16, 4, None, None, None, fake, wx - 1, 0, 2, None, None) == EWORK
+    assert lib.pg_eps_inverse_mixed_workspace(16, 4, 2) < wx                               # two frequencies at a time
