@@ -196,3 +196,30 @@ def test_polarization_entry_points_validate_on_the_host():
     assert lib.pg_eps_inverse_mixed(fake, 16, 4, None, None, None, fake, big, 0, 3, None, None) == EARG
     assert lib.pg_eps_inverse_mixed(fake, 16, 4, None, None, None, fake, wx - 1, 0, 2, None, None) == EWORK
     assert lib.pg_eps_inverse_mixed_workspace(16, 4, 2) < wx                               # two frequencies at a time
+
+
+def test_batch_tuner_keeps_the_fastest_choice_per_shape_class(tmp_path):
+    """The batch autotuner (host logic): the fastest candidate per shape class
+    wins, is written to the JSON file, and a tuner loaded from that file
+    returns it without timing anything again; the key bins N to 256 and K to
+    65,536 so nearby shapes share a choice."""
+    from pygw_gb300.batch import Tuner
+    path = str(tmp_path / "tune.json")
+    times = {(8, 1): 5.0, (8, 2): 3.0, (16, 2): 4.0}
+    seen = []
+
+    def timer(kc, wb):
+        seen.append((kc, wb))
+        return times[(kc, wb)]
+
+    t = Tuner(path)
+    key = Tuner.key(1200, 23, 192, 216, 953856, 48)
+    assert key == Tuner.key(1100, 23, 192, 216, 953856 - 1000, 48) != Tuner.key(1300, 23, 192, 216, 953856, 48)
+    c = t.choose(key, list(times), timer)
+    assert (c.k_chunk, c.omega_batch, c.ms_per_omega) == (8, 2, 3.0) and seen == list(times)
+
+    def no_timer(kc, wb):
+        raise AssertionError("a stored choice must not be timed again")
+
+    c2 = Tuner(path).choose(key, list(times), no_timer)
+    assert (c2.k_chunk, c2.omega_batch) == (8, 2)
