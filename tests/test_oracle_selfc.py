@@ -101,3 +101,35 @@ def test_svd_convolution_is_linear_in_the_basis():
     # a basis function convolved alone is fr_convolution2 of it
     want = osc.fr_convolution2(enk[2], Ul[0], Ul[0, 5], om, om[5], wom)
     assert cnl[0, 2, 5] == want
+
+
+def test_spline_matrix_applies_the_reference_spline():
+    """S·y is the cubic spline of y with the boundary conditions of
+    mcommon.py:135 (second derivative 0 at the first point, slope 0 at the
+    last, extrapolating), evaluated on the dense mesh — for any data y."""
+    from scipy import interpolate
+
+    from pygw_gb300.selfc import spline_matrix
+    rng = np.random.default_rng(3)
+    omega = np.sort(rng.uniform(0.01, 50.0, 24))
+    dense = np.concatenate([np.linspace(0.005, 60.0, 200), omega])
+    S = spline_matrix(omega, dense)
+    assert S.shape == (dense.size, omega.size)
+    y = rng.standard_normal((omega.size, 3))
+    ref = interpolate.CubicSpline(omega, y, axis=0, bc_type=((2, np.zeros(3)), (1, np.zeros(3))),
+                                  extrapolate=True)(dense)
+    assert np.allclose(S @ y, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+    # at the nodes the spline interpolates
+    assert np.allclose(S[200:], np.eye(omega.size), atol=1e-12)
+
+
+def test_selfc_k_chunk_fits_the_budget():
+    """The self-energy's k-chunk and frequency batch keep the split-precision
+    workspace within the budget (host arithmetic and size queries only)."""
+    from pygw_gb300 import _lib
+    from pygw_gb300.selfc import mixed_k_chunk
+    lib = _lib.load()
+    for P, npb, nom, budget in [(3200, 1200, 48, 64 << 30), (3200, 1200, 48, 8 << 30), (90, 128, 16, 1 << 30)]:
+        nk, nb = mixed_k_chunk(P, npb, nom, budget=budget)
+        assert nk >= 1 and 1 <= nb <= nom
+        assert nb == 1 or lib.pg_selfc_mwm_workspace(nk, P, npb, nb, 1) <= budget
