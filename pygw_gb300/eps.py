@@ -213,18 +213,21 @@ def _all_k_device(minm, nkp, P, npb):
     return out
 
 
-def mixed_omega_batch(nb1, nb2, nkp, npb, nom, budget_bytes=None):
+def mixed_omega_batch(nb1, nb2, nkp, npb, nom, budget_bytes=None, sm_count=None):
     """Frequencies per launch of the split-precision χ0: the fewest that give
     the digit GEMM two waves of 2-CTA clusters, within a memory budget
     (default: 40 % of the free device memory).  Fewer frequencies per launch
     leave more of L2 to the digit planes they share: at N_PB 1200 and 6³ k one
     frequency per launch reads 427 GB from DRAM per frequency, two 525 GB, four
-    567 GB, and runs 7 % faster than two."""
+    567 GB, and runs 7 % faster than two.  ``sm_count`` defaults to the
+    current device's."""
     lib = _lib.load()
     if budget_bytes is None:
         free, _ = torch.cuda.mem_get_info()
         budget_bytes = int(0.4 * free)
-    clusters = max(1, torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count // 2)
+    if sm_count is None:
+        sm_count = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    clusters = max(1, sm_count // 2)
     offs = (ctypes.c_size_t * 9)()
     dims = (ctypes.c_longlong * 9)()
     wb = 1

@@ -223,3 +223,21 @@ def test_batch_tuner_keeps_the_fastest_choice_per_shape_class(tmp_path):
 
     c2 = Tuner(path).choose(key, list(times), no_timer)
     assert (c2.k_chunk, c2.omega_batch) == (8, 2)
+
+
+def test_mixed_omega_batch_is_the_fewest_frequencies_filling_two_waves():
+    """Host logic of the split-precision frequency batch: the fewest
+    frequencies per launch (doubling) whose work units fill two waves of
+    2-CTA clusters on 152 SMs, within the memory budget.  At C3 (55 blocks ×
+    4 K splits) one frequency already gives 220 units; a small problem needs
+    more frequencies; a tight budget stops the doubling."""
+    from pygw_gb300 import eps as peps
+    big = 1 << 45
+    assert peps.mixed_omega_batch(23, 192, 216, 1200, 48, budget_bytes=big, sm_count=152) == 1
+    wb_small = peps.mixed_omega_batch(9, 24, 8, 128, 16, budget_bytes=big, sm_count=152)
+    assert wb_small > 1 and wb_small & (wb_small - 1) == 0 and wb_small <= 16
+    from pygw_gb300 import _lib
+    lib = _lib.load()
+    tight = lib.pg_chi0_mixed_workspace(9, 24, 8, 128, 2, 0)           # room for one doubling only
+    assert peps.mixed_omega_batch(9, 24, 8, 128, 16, budget_bytes=tight, sm_count=152) == min(2, wb_small)
+    assert peps.mixed_omega_batch(9, 24, 8, 128, 3, budget_bytes=big, sm_count=152) <= 3
