@@ -1,0 +1,136 @@
+"""Generate golden vectors for calc_eps from the reference's own code.
+
+Run in a container that holds the reference at /root/reference:
+
+    python tests/golden/make_calc_eps_golden.py
+
+The reference's driver is Python 2 with f2py modules, so it cannot be
+imported here.  This script reads the text of
+``MatrixElements2Band.calc_eps`` (pygw.py:3039-3297) at run time, rewrites
+its Python 2 print statements as print() calls (nothing else is changed),
+and runs the method with numpy/scipy in place of the reference's star
+imports and with small stand-in objects for the parts of the reference that
+are not on this path (the product basis, the mesh and band objects, and
+``calc_minm``, which returns seeded random matrix elements).  The weights
+``kcw`` are seeded random numbers too: the contraction does not depend on
+where they come from.  The inputs and the reference's outputs are written to
+``calc_eps_golden.npz`` beside this script; nothing of the reference's source
+is stored.
+
+Cases: a finite q, q = 0 (head and wings from seeded momentum matrix
+elements), and q = 0 in an SVD frequency basis (Ul, dUl).
+"""
+import io
+import itertools
+import os
+import re
+import sys
+import textwrap
+import timeit
+
+import numpy as np
+import scipy.linalg
+
+REF = "/root/reference/pygw.py"
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "calc_eps_golden.npz")
+
+
+def load_calc_eps():
+    lines = open(REF).read().split("\n")
+    start = next(i for i, l in enumerate(lines) if l.startswith("    def calc_eps(self,"))
+    end = next(i for i in range(start + 1, len(lines)) if lines[i].startswith("    def "))
+    src = []
+    for l in lines[start:end]:
+        m = re.match(r"^(\s*)print\s*>>\s*(\w+)\s*,\s*(.+)$", l)
+        if m:
+            l = f"{m.group(1)}print({m.group(3)}, file={m.group(2)})"
+        else:
+            m = re.match(r"^(\s*)print\s+(?!\()(.+)$", l)
+            if m:
+                l = f"{m.group(1)}print({m.group(2)})"
+        src.append(l)
+    code = textwrap.dedent("\n".join(src))
+    ns = {}
+    exec("from numpy import *", ns)
+    ns.update(linalg=scipy.linalg, la=np.linalg, timer=timeit.default_timer, itertools=itertools, sys=sys,
+              Save_eps=False, ForceReal=False, save=np.save)
+    exec(compile(code, REF + ":calc_eps", "exec"), ns)
+    return ns["calc_eps"]
+
+
+class NS:
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+
+def case(rng, iq, nkp, nvbm, ncbm, nb2, npb, nom, nl=None):
+    """Inputs in the reference's layouts and the reference's calc_eps result."""
+    nbmaxpol = ncbm + nb2
+    nb1 = nvbm                                     # ncg_p = 0: no core states
+    nw = nom if nl is None else nl                 # kcw's last axis: frequencies or basis functions
+    M = 0.08 * (rng.standard_normal((nkp, nb1, nb2, npb)) + 1j * rng.standard_normal((nkp, nb1, nb2, npb)))
+    kcw = np.asfortranarray(rng.uniform(0.0, 1.0, (nb1, nb2, nkp, nw)))
+    Ebnd = np.sort(rng.uniform(-1.0, 2.0, (1, nkp, nbmaxpol)), axis=2)
+    Ebnd[0, :, :nvbm] -= 1.0                       # occupied below the empty bands
+    Vol = 250.0
+    omega = np.geomspace(0.01, 10.0, nom)
+    Ul = dUl = None
+    if nl is not None:
+        Ul = rng.standard_normal((nl, nom)) / np.sqrt(nom)
+        dUl = np.linalg.pinv(Ul)                   # (nom, nl)
+    head_in = mmatvv = pm = None
+    if iq == 0:
+        head_in = (rng.uniform(0.5, 2.0, nw) + 0.1j * rng.standard_normal(nw)).astype(complex)
+        mmatvv = 0.3 * (rng.standard_normal((nkp, nbmaxpol, nvbm, 3)) + 1j * rng.standard_normal((nkp, nbmaxpol, nvbm, 3)))
+        # pm as pygw.py:3119-3141 forms it (restated to hand the same vector to the oracle)
+        coefw = 2.0 * np.sqrt(np.pi / Vol)
+        pm = np.zeros((nkp, nb1 * nb2), dtype=complex)
+        for ik in range(nkp):
+            mmv = np.sum(mmatvv[ik, ncbm:nbmaxpol, :, :], axis=2) * (coefw / np.sqrt(3.0))
+            ie12 = 0
+            for ie1 in range(nvbm):
+                for ie2 in range(ncbm, nbmaxpol):
+                    edif = Ebnd[0, ik, ie1] - Ebnd[0, ik, ie2]
+                    if abs(edif) > 1e-10:
+                        pm[ik, ie12] = mmv[ie2 - ncbm, ie1] / edif
+                    ie12 += 1
+
+    me = NS(barcvm=np.zeros((1, npb)),
+            calc_minm=lambda ik, *a: (M[ik].copy(), None))
+    strc = NS(nat=1)
+    pb = NS(big_l=[[0, 1]])
+    pw = NS(inverse_indgq=lambda q: None)
+    kqm = NS(qlistc=np.zeros((2, 3), dtype=int), LCMq=1, kii_ind=np.arange(nkp), kqid=np.zeros((nkp, 2), dtype=int))
+    ks = NS(nomax_numin=(nvbm - 1, ncbm), ncg_p=0, nbmaxpol=nbmaxpol, Ebnd=Ebnd)
+    core = NS(corind=np.zeros((0, 3), dtype=int), eig_core=[[]])
+    latgen = NS(Vol=Vol)
+    fr = NS(omega=omega)
+    hq = None
+    if iq == 0:
+        mmatcv = np.zeros((nkp, nbmaxpol, 0, 3), dtype=complex)
+        hq = (head_in.copy(), mmatcv, mmatvv, 0)
+    fout = io.StringIO()
+    eps, epsw1, epsw2, head = load_calc_eps()(me, iq, hq, strc, None, latgen, kqm, ks, None, pw, pb, core, None, fr,
+                                                kcw, "", dUl, Ul, fout)
+    out = dict(M=M, kcw=kcw, eps=np.asarray(eps))
+    if iq == 0:
+        out.update(pm=pm, head_in=head_in, epsw1=epsw1, epsw2=epsw2, head=np.asarray(head))
+    if nl is not None:
+        out.update(Ul=Ul, dUl=dUl)
+    return out
+
+
+def main():
+    rng = np.random.default_rng(20261203)
+    cases = {
+        "q": case(rng, 1, nkp=6, nvbm=3, ncbm=3, nb2=5, npb=24, nom=4),
+        "q0": case(rng, 0, nkp=6, nvbm=3, ncbm=3, nb2=5, npb=24, nom=4),
+        "q0svd": case(rng, 0, nkp=6, nvbm=3, ncbm=3, nb2=5, npb=24, nom=6, nl=4),
+    }
+    flat = {f"{c}.{k}": v for c, d in cases.items() for k, v in d.items()}
+    np.savez_compressed(OUT, **flat)
+    print(f"wrote {OUT}: " + ", ".join(f"{k}{tuple(v.shape)}" for k, v in flat.items()))
+
+
+if __name__ == "__main__":
+    main()
