@@ -1,9 +1,12 @@
 """numpy restatement of the χ0 contraction and ε⁻¹ (test infrastructure).
 
-Parity unpinned: the reference ships no tests, fixtures or golden vectors for this
-path and cannot be built or run here (Fortran without a compiler, Python 2 with
-f2py modules); this restatement is pinned by known answers instead
-(tests/test_oracle_*.py).
+Pinned against the reference's own calc_eps: the reference ships no tests or
+golden vectors and its driver (Python 2 with f2py modules) cannot be imported,
+so tests/golden/make_calc_eps_golden.py runs the text of calc_eps itself (print
+statements rewritten) on seeded inputs and stores its outputs; this
+restatement reproduces them exactly for a finite q, q = 0 with head and wings,
+and the SVD basis (tests/test_oracle_eps_golden.py).  Known answers
+(tests/test_oracle_eps.py) check it as well.
 
 Follows MatrixElements2Band.calc_eps (pygw.py:3039-3297) for a Γ-point or
 finite q, with or without the SVD frequency basis:

@@ -1,9 +1,13 @@
 """numpy restatement of the correlation self-energy contraction (test infrastructure).
 
-Parity unpinned: the reference ships no tests, fixtures or golden vectors for this
-path and cannot be built or run here (Fortran without a compiler, Python 2 with
-f2py modules); this restatement is pinned by known answers instead
-(tests/test_oracle_*.py).
+Pinned in two ways.  The Python parts of the reference — the mwm contraction
+with its q = 0 terms, the energies at k − q, the iopfreq 4 interpolation and
+the SVD-branch product — are checked against golden vectors from the
+reference's own calc_selfc and Compute_selfc_inside, run on seeded inputs by
+tests/golden/make_calc_selfc_golden.py (tests/test_oracle_selfc_golden.py).
+The Fortran convolution kernels (fnc.f90) cannot be built here (no Fortran
+compiler); their restatement below is pinned by known answers
+(tests/test_oracle_selfc.py).
 
 Follows MatrixElements2Band.calc_selfc (pygw.py:3299-3412) for one q and the
 frequency convolution it calls (mcommon.py:80-131 → fnc.f90:90-177):

@@ -16,6 +16,7 @@ par3 weights and the basis changes around ε⁻¹.
 from __future__ import annotations
 
 import numpy as np
+import scipy.linalg
 import scipy.optimize
 import torch
 
@@ -50,7 +51,7 @@ def svd_functions(iomega, wiomeg, om_min, om_max, om_nom, svd_cutoff):
     iw = np.concatenate([-iomega[::-1], iomega])
     dw = np.concatenate([wiomeg[::-1], wiomeg])
     K = (om * dom / np.pi)[None, :] * np.sqrt(dw)[:, None] / (om[None, :] ** 2 + iw[:, None] ** 2)
-    u, s, _ = np.linalg.svd(K, full_matrices=True)
+    u, s, _ = scipy.linalg.svd(K, full_matrices=True)          # the reference's routine (pygw.py:3490)
     small = np.where(s < svd_cutoff)[0]
     n = int(small[0]) if len(small) else len(s)
     Ul = u[:, :n].T / np.sqrt(dw)[None, :]

@@ -1,0 +1,81 @@
+"""Generate golden vectors for the SVD frequency basis from the reference's own code.
+
+Run in a container that holds the reference at /root/reference:
+
+    python tests/golden/make_svd_golden.py
+
+Runs the text of ``svd_functions`` (pygw.py:3478-3501) and of
+``Give2TanMesh`` (mcommon.py:13-31) on two Matsubara meshes.  Two Python 2
+forms are rewritten: print statements become print() calls, and the integer
+division ``len(iom)/2`` becomes ``len(iom)//2`` (what it computes under
+Python 2).  The reference's ``linalg`` there is scipy.linalg.  Output:
+``svd_golden.npz`` beside this script.
+"""
+import io
+import os
+import re
+import textwrap
+import warnings
+
+import numpy as np
+import scipy.linalg
+import scipy.optimize
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PYGW = "/root/reference/pygw.py"
+MCOMMON = "/root/reference/mcommon.py"
+OUT = os.path.join(HERE, "svd_golden.npz")
+
+
+def _extract(path, head, indent):
+    lines = open(path).read().split("\n")
+    start = next(i for i, l in enumerate(lines) if l.startswith(head))
+    end = next((i for i in range(start + 1, len(lines))
+                if lines[i].strip() and not lines[i].lstrip().startswith("#")
+                and not lines[i].startswith(indent + " ")), len(lines))
+    out = []
+    for l in lines[start:end]:
+        m = re.match(r"^(\s*)print\s*>>\s*(\w+)\s*,\s*(.+)$", l)
+        if m:
+            l = f"{m.group(1)}print({m.group(3)}, file={m.group(2)})"
+        out.append(l.replace("len(iom)/2", "len(iom)//2"))
+    return textwrap.dedent("\n".join(out))
+
+
+class NS:
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+
+def load():
+    ns = {}
+    exec("from numpy import *", ns)
+    ns.update(optimize=scipy.optimize, linalg=scipy.linalg)
+    exec(compile(_extract(MCOMMON, "def Give2TanMesh(", ""), MCOMMON + ":Give2TanMesh", "exec"), ns)
+    ns["mcmn"] = NS(Give2TanMesh=ns["Give2TanMesh"])
+    exec(compile(_extract(PYGW, "def svd_functions(", ""), PYGW + ":svd_functions", "exec"), ns)
+    return ns["Give2TanMesh"], ns["svd_functions"]
+
+
+def main():
+    warnings.filterwarnings("ignore", category=SyntaxWarning)
+    give2tan, svd_functions = load()
+    out = {}
+    for name, (nom, om_min, om_max, om_nom, cut) in {
+            "a": (32, 1e-3, 20.0, 60, 1e-10),
+            "b": (48, 5e-4, 40.0, 80, 1e-8)}.items():
+        x = np.polynomial.legendre.leggauss(nom)
+        t = 0.5 * (x[0] + 1.0)
+        iomega = 0.02 * t / (1.0 - t + 1e-3)                   # a Matsubara-like mesh, dense near 0
+        wiomeg = 0.02 * 0.5 * x[1] * (1.0 + 1e-3) / (1.0 - t + 1e-3) ** 2
+        om, dom = give2tan(om_min, om_max, om_nom)
+        Ul, dUl = svd_functions(iomega, wiomeg, om_min, om_max, om_nom, cut, io.StringIO())
+        out.update({f"{name}.iomega": iomega, f"{name}.wiomeg": wiomeg,
+                    f"{name}.args": np.array([om_min, om_max, om_nom, cut]),
+                    f"{name}.om": om, f"{name}.dom": dom, f"{name}.Ul": Ul, f"{name}.dUl": dUl})
+    np.savez_compressed(OUT, **out)
+    print(f"wrote {OUT}: " + ", ".join(f"{k}{tuple(np.shape(v))}" for k, v in out.items()))
+
+
+if __name__ == "__main__":
+    main()
