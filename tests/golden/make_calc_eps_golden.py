@@ -35,12 +35,27 @@ REF = "/root/reference/pygw.py"
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "calc_eps_golden.npz")
 
 
+def _split_comment(line):
+    """(code, comment) of a source line: the first # outside a string literal."""
+    quote = None
+    for i, ch in enumerate(line):
+        if quote:
+            if ch == quote and line[i - 1] != "\\":
+                quote = None
+        elif ch in "'\"":
+            quote = ch
+        elif ch == "#":
+            return line[:i].rstrip(), "  " + line[i:]
+    return line, ""
+
+
 def load_calc_eps():
     lines = open(REF).read().split("\n")
     start = next(i for i, l in enumerate(lines) if l.startswith("    def calc_eps(self,"))
     end = next(i for i in range(start + 1, len(lines)) if lines[i].startswith("    def "))
     src = []
     for l in lines[start:end]:
+        l, comment = _split_comment(l)
         m = re.match(r"^(\s*)print\s*>>\s*(\w+)\s*,\s*(.+)$", l)
         if m:
             l = f"{m.group(1)}print({m.group(3)}, file={m.group(2)})"

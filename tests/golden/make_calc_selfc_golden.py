@@ -40,9 +40,24 @@ MCOMMON = "/root/reference/mcommon.py"
 OUT = os.path.join(HERE, "calc_selfc_golden.npz")
 
 
+def _split_comment(line):
+    """(code, comment) of a source line: the first # outside a string literal."""
+    quote = None
+    for i, ch in enumerate(line):
+        if quote:
+            if ch == quote and line[i - 1] != "\\":
+                quote = None
+        elif ch in "'\"":
+            quote = ch
+        elif ch == "#":
+            return line[:i].rstrip(), "  " + line[i:]
+    return line, ""
+
+
 def _py3(lines):
     out = []
     for l in lines:
+        l, comment = _split_comment(l)
         m = re.match(r"^(\s*)print\s*>>\s*(\w+)\s*,\s*(.+)$", l)
         if m:
             l = f"{m.group(1)}print({m.group(3)}, file={m.group(2)})"

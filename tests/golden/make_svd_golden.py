@@ -27,6 +27,20 @@ MCOMMON = "/root/reference/mcommon.py"
 OUT = os.path.join(HERE, "svd_golden.npz")
 
 
+def _split_comment(line):
+    """(code, comment) of a source line: the first # outside a string literal."""
+    quote = None
+    for i, ch in enumerate(line):
+        if quote:
+            if ch == quote and line[i - 1] != "\\":
+                quote = None
+        elif ch in "'\"":
+            quote = ch
+        elif ch == "#":
+            return line[:i].rstrip(), "  " + line[i:]
+    return line, ""
+
+
 def _extract(path, head, indent):
     lines = open(path).read().split("\n")
     start = next(i for i, l in enumerate(lines) if l.startswith(head))
@@ -35,6 +49,7 @@ def _extract(path, head, indent):
                 and not lines[i].startswith(indent + " ")), len(lines))
     out = []
     for l in lines[start:end]:
+        l, comment = _split_comment(l)
         m = re.match(r"^(\s*)print\s*>>\s*(\w+)\s*,\s*(.+)$", l)
         if m:
             l = f"{m.group(1)}print({m.group(3)}, file={m.group(2)})"
