@@ -8,7 +8,7 @@ Parity: the reference ships no tests or golden vectors and its driver (Python 2
 with f2py modules) cannot be imported.  Its numpy parts — calc_eps and the
 Python around the self-energy convolutions — are run from their source text on
 seeded inputs by the scripts in tests/golden/, and the restatements here
-reproduce those outputs (tests/test_oracle_*_golden.py).  Its Fortran parts —
+reproduce those outputs (tests/test_*golden.py).  Its Fortran parts —
 the tetrahedron weights and the convolution kernels — cannot be built (no
 Fortran compiler); their restatements are pinned by known answers
 (tests/test_oracle_*.py).
