@@ -23,59 +23,25 @@ elements), and q = 0 in an SVD frequency basis (Ul, dUl).
 import io
 import itertools
 import os
-import re
 import sys
-import textwrap
 import timeit
 
 import numpy as np
 import scipy.linalg
 
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from refsrc import NS, load  # noqa: E402
+
 REF = "/root/reference/pygw.py"
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "calc_eps_golden.npz")
 
 
-def _split_comment(line):
-    """(code, comment) of a source line: the first # outside a string literal."""
-    quote = None
-    for i, ch in enumerate(line):
-        if quote:
-            if ch == quote and line[i - 1] != "\\":
-                quote = None
-        elif ch in "'\"":
-            quote = ch
-        elif ch == "#":
-            return line[:i].rstrip(), "  " + line[i:]
-    return line, ""
-
-
 def load_calc_eps():
-    lines = open(REF).read().split("\n")
-    start = next(i for i, l in enumerate(lines) if l.startswith("    def calc_eps(self,"))
-    end = next(i for i in range(start + 1, len(lines)) if lines[i].startswith("    def "))
-    src = []
-    for l in lines[start:end]:
-        l, comment = _split_comment(l)
-        m = re.match(r"^(\s*)print\s*>>\s*(\w+)\s*,\s*(.+)$", l)
-        if m:
-            l = f"{m.group(1)}print({m.group(3)}, file={m.group(2)})"
-        else:
-            m = re.match(r"^(\s*)print\s+(?!\()(.+)$", l)
-            if m:
-                l = f"{m.group(1)}print({m.group(2)})"
-        src.append(l)
-    code = textwrap.dedent("\n".join(src))
     ns = {}
     exec("from numpy import *", ns)
     ns.update(linalg=scipy.linalg, la=np.linalg, timer=timeit.default_timer, itertools=itertools, sys=sys,
               Save_eps=False, ForceReal=False, save=np.save)
-    exec(compile(code, REF + ":calc_eps", "exec"), ns)
-    return ns["calc_eps"]
-
-
-class NS:
-    def __init__(self, **kw):
-        self.__dict__.update(kw)
+    return load(REF, "    def calc_eps(self,", "    ", ns, "calc_eps")
 
 
 def case(rng, iq, nkp, nvbm, ncbm, nb2, npb, nom, nl=None):

@@ -21,9 +21,7 @@ pinned by known answers in tests/test_oracle_selfc.py).  Output:
 import io
 import itertools
 import os
-import re
 import sys
-import textwrap
 import timeit
 import warnings
 
@@ -34,55 +32,13 @@ import scipy.linalg
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from oracle import selfc as osc  # noqa: E402
+sys.path.insert(0, HERE)
+import refsrc  # noqa: E402
+from refsrc import NS  # noqa: E402
 
 PYGW = "/root/reference/pygw.py"
 MCOMMON = "/root/reference/mcommon.py"
 OUT = os.path.join(HERE, "calc_selfc_golden.npz")
-
-
-def _split_comment(line):
-    """(code, comment) of a source line: the first # outside a string literal."""
-    quote = None
-    for i, ch in enumerate(line):
-        if quote:
-            if ch == quote and line[i - 1] != "\\":
-                quote = None
-        elif ch in "'\"":
-            quote = ch
-        elif ch == "#":
-            return line[:i].rstrip(), "  " + line[i:]
-    return line, ""
-
-
-def _py3(lines):
-    out = []
-    for l in lines:
-        l, comment = _split_comment(l)
-        m = re.match(r"^(\s*)print\s*>>\s*(\w+)\s*,\s*(.+)$", l)
-        if m:
-            l = f"{m.group(1)}print({m.group(3)}, file={m.group(2)})"
-        else:
-            m = re.match(r"^(\s*)print\s+(?!\()(.+)$", l)
-            if m:
-                l = f"{m.group(1)}print({m.group(2)})"
-        out.append(l)
-    return textwrap.dedent("\n".join(out))
-
-
-def _extract(path, head, indent):
-    """The function that starts with ``head`` (at ``indent``), up to the first
-    code line indented no deeper than its def."""
-    lines = open(path).read().split("\n")
-    start = next(i for i, l in enumerate(lines) if l.startswith(head))
-    end = next((i for i in range(start + 1, len(lines))
-                if lines[i].strip() and not lines[i].lstrip().startswith("#")
-                and not lines[i].startswith(indent + " ")), len(lines))
-    return _py3(lines[start:end])
-
-
-class NS:
-    def __init__(self, **kw):
-        self.__dict__.update(kw)
 
 
 def _fnc(enks):
@@ -113,10 +69,8 @@ def load(saved, enks):
     ns.update(interpolate=scipy.interpolate, linalg=scipy.linalg, la=np.linalg, timer=timeit.default_timer,
               itertools=itertools, sys=sys, FORT=True, fnc=_fnc(enks),
               save=lambda path, a: saved.append(np.array(a)))
-    exec(compile(_extract(MCOMMON, "def Compute_selfc_inside(", ""), MCOMMON + ":Compute_selfc_inside", "exec"), ns)
-    ns["mcmn"] = NS(Compute_selfc_inside=ns["Compute_selfc_inside"])
-    exec(compile(_extract(PYGW, "    def calc_selfc(self,", "    "), PYGW + ":calc_selfc", "exec"), ns)
-    return ns["calc_selfc"]
+    ns["mcmn"] = NS(Compute_selfc_inside=refsrc.load(MCOMMON, "def Compute_selfc_inside(", "", ns, "Compute_selfc_inside"))
+    return refsrc.load(PYGW, "    def calc_selfc(self,", "    ", ns, "calc_selfc")
 
 
 def case(rng, iq, npb=16, nkp=4, ibgw=1, nbgw=3, ncg_c=1, nbands_c=6, nom=5, nl=None, dense=False):

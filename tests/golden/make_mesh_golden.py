@@ -18,8 +18,7 @@ this script (tetc, kqid and the chosen diagonal per case).
 import io
 import itertools
 import os
-import re
-import textwrap
+import sys
 import timeit
 import warnings
 from functools import reduce
@@ -27,43 +26,12 @@ from functools import reduce
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import refsrc  # noqa: E402
+from refsrc import NS  # noqa: E402
+
 KQMESH = "/root/reference/kqmesh.py"
 OUT = os.path.join(HERE, "mesh_golden.npz")
-
-
-def _split_comment(line):
-    """(code, comment) of a source line: the first # outside a string literal."""
-    quote = None
-    for i, ch in enumerate(line):
-        if quote:
-            if ch == quote and line[i - 1] != "\\":
-                quote = None
-        elif ch in "'\"":
-            quote = ch
-        elif ch == "#":
-            return line[:i].rstrip(), "  " + line[i:]
-    return line, ""
-
-
-def _extract(path, head, indent):
-    lines = open(path).read().split("\n")
-    start = next(i for i, l in enumerate(lines) if l.startswith(head))
-    end = next((i for i in range(start + 1, len(lines))
-                if lines[i].strip() and not lines[i].lstrip().startswith("#")
-                and not lines[i].startswith(indent + " ")), len(lines))
-    out = []
-    for l in lines[start:end]:
-        l, comment = _split_comment(l)
-        m = re.match(r"^(\s*)print\s*>>\s*(\w+)\s*,\s*(.+)$", l)
-        if m:
-            l = f"{m.group(1)}print({m.group(3)}, file={m.group(2)})"
-        else:
-            m = re.match(r"^(\s*)print\s+(?!\()(.+)$", l)
-            if m:
-                l = f"{m.group(1)}print({m.group(2)})"
-        l = re.sub(r"(\w+)\.has_key\(([^()]*)\)", r"(\2 in \1)", l)
-        out.append(l)
-    return textwrap.dedent("\n".join(out))
 
 
 class Mesh:
@@ -92,18 +60,12 @@ class Mesh:
         return np.array([k0, k1, k2])
 
 
-class NS:
-    def __init__(self, **kw):
-        self.__dict__.update(kw)
-
-
 def load():
     ns = {}
     exec("from numpy import *", ns)
     ns.update(itertools=itertools, timer=timeit.default_timer, FORT=False, reduce=reduce, lcm=np.lcm,
               fkp=NS(k2indx=lambda k, div: (k[0] * div[1] + k[1]) * div[2] + k[2]))
-    exec(compile(_extract(KQMESH, "    def tetra(self,", "    "), KQMESH + ":tetra", "exec"), ns)
-    return ns["tetra"]
+    return refsrc.load(KQMESH, "    def tetra(self,", "    ", ns, "tetra")
 
 
 def main():

@@ -15,54 +15,17 @@ product's host code must reproduce.  Output: ``polarization_weights_golden.npz``
 """
 import io
 import os
-import re
-import textwrap
+import sys
 import warnings
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+from refsrc import NS, load  # noqa: E402
+
 PYGW = "/root/reference/pygw.py"
 OUT = os.path.join(HERE, "polarization_weights_golden.npz")
-
-
-def _split_comment(line):
-    """(code, comment) of a source line: the first # outside a string literal."""
-    quote = None
-    for i, ch in enumerate(line):
-        if quote:
-            if ch == quote and line[i - 1] != "\\":
-                quote = None
-        elif ch in "'\"":
-            quote = ch
-        elif ch == "#":
-            return line[:i].rstrip(), "  " + line[i:]
-    return line, ""
-
-
-def _extract(path, head, indent):
-    lines = open(path).read().split("\n")
-    start = next(i for i, l in enumerate(lines) if l.startswith(head))
-    end = next((i for i in range(start + 1, len(lines))
-                if lines[i].strip() and not lines[i].lstrip().startswith("#")
-                and not lines[i].startswith(indent + " ")), len(lines))
-    out = []
-    for l in lines[start:end]:
-        l, _ = _split_comment(l)
-        m = re.match(r"^(\s*)print\s*>>\s*(\w+)\s*,\s*(.+)$", l)
-        if m:
-            l = f"{m.group(1)}print({m.group(3)}, file={m.group(2)})"
-        else:
-            m = re.match(r"^(\s*)print\s+(?!\()(.+)$", l)
-            if m:
-                l = f"{m.group(1)}print({m.group(2)})"
-        out.append(l)
-    return textwrap.dedent("\n".join(out))
-
-
-class NS:
-    def __init__(self, **kw):
-        self.__dict__.update(kw)
 
 
 def main():
@@ -80,8 +43,7 @@ def main():
     ns = {}
     exec("from numpy import *", ns)
     ns.update(ft=NS(bz_calcqdepw_par2=par2, bz_calcqdepw_par3=par3), sys=NS(exit=lambda *a: None))
-    exec(compile(_extract(PYGW, "def Polarization_weights(", ""), PYGW + ":Polarization_weights", "exec"), ns)
-    pw = ns["Polarization_weights"]
+    pw = load(PYGW, "def Polarization_weights(", "", ns, "Polarization_weights")
 
     rng = np.random.default_rng(20261205)
     nkp, nirkp, ncg_p, nbmaxpol = 8, 5, 2, 7

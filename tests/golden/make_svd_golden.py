@@ -13,8 +13,7 @@ Python 2).  The reference's ``linalg`` there is scipy.linalg.  Output:
 """
 import io
 import os
-import re
-import textwrap
+import sys
 import warnings
 
 import numpy as np
@@ -22,54 +21,22 @@ import scipy.linalg
 import scipy.optimize
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import refsrc  # noqa: E402
+from refsrc import NS  # noqa: E402
+
 PYGW = "/root/reference/pygw.py"
 MCOMMON = "/root/reference/mcommon.py"
 OUT = os.path.join(HERE, "svd_golden.npz")
-
-
-def _split_comment(line):
-    """(code, comment) of a source line: the first # outside a string literal."""
-    quote = None
-    for i, ch in enumerate(line):
-        if quote:
-            if ch == quote and line[i - 1] != "\\":
-                quote = None
-        elif ch in "'\"":
-            quote = ch
-        elif ch == "#":
-            return line[:i].rstrip(), "  " + line[i:]
-    return line, ""
-
-
-def _extract(path, head, indent):
-    lines = open(path).read().split("\n")
-    start = next(i for i, l in enumerate(lines) if l.startswith(head))
-    end = next((i for i in range(start + 1, len(lines))
-                if lines[i].strip() and not lines[i].lstrip().startswith("#")
-                and not lines[i].startswith(indent + " ")), len(lines))
-    out = []
-    for l in lines[start:end]:
-        l, comment = _split_comment(l)
-        m = re.match(r"^(\s*)print\s*>>\s*(\w+)\s*,\s*(.+)$", l)
-        if m:
-            l = f"{m.group(1)}print({m.group(3)}, file={m.group(2)})"
-        out.append(l.replace("len(iom)/2", "len(iom)//2"))
-    return textwrap.dedent("\n".join(out))
-
-
-class NS:
-    def __init__(self, **kw):
-        self.__dict__.update(kw)
 
 
 def load():
     ns = {}
     exec("from numpy import *", ns)
     ns.update(optimize=scipy.optimize, linalg=scipy.linalg)
-    exec(compile(_extract(MCOMMON, "def Give2TanMesh(", ""), MCOMMON + ":Give2TanMesh", "exec"), ns)
-    ns["mcmn"] = NS(Give2TanMesh=ns["Give2TanMesh"])
-    exec(compile(_extract(PYGW, "def svd_functions(", ""), PYGW + ":svd_functions", "exec"), ns)
-    return ns["Give2TanMesh"], ns["svd_functions"]
+    give2tan = refsrc.load(MCOMMON, "def Give2TanMesh(", "", ns, "Give2TanMesh")
+    ns["mcmn"] = NS(Give2TanMesh=give2tan)
+    return give2tan, refsrc.load(PYGW, "def svd_functions(", "", ns, "svd_functions", replace=[("len(iom)/2", "len(iom)//2")])
 
 
 def main():
