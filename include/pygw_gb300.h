@@ -71,8 +71,10 @@ int pg_bz_calcqdepw_par3(const double* enk, int nbnd, int nkp, double ef, const 
  * frequencies are processed in chunks that fit.  Returns PG_ETOOBIG when the
  * k lists plus one frequency of scratch (4*ntet*nb1*nb2 doubles) do not fit.
  * All calls share that array: calls that overlap on the GPU race and must be
- * serialised.  The first call on a device looks up the array's device address
- * and caches it; make that call before any stream capture. */
+ * serialised.  The first call in a device context looks up the array's
+ * device address and caches it under the context's id (a reset device or a
+ * new context gets a fresh lookup); make that call before any stream
+ * capture. */
 size_t pg_bz_calcqdepw_par2_noalloc_capacity(void);
 int pg_bz_calcqdepw_par2_noalloc(const double* enk, int nbnd, int nkp, double ef, const int* kqid, int ncg,
                                  int nomx, int numin, const double* omega, int nom, const int* tetc, int ntet,
@@ -216,6 +218,18 @@ int pg_selfc_convolution_svd(const void* mwm, int nk, int nb1, int nb2, int nl, 
  * Number of kernels this library has enqueued since it was loaded (all entry
  * points, all streams).  No counterpart in the reference. */
 unsigned long long pg_launch_count(void);
+
+/* Limit, in nanoseconds of the GPU's global timer, of one pipeline wait
+ * inside the split-precision digit GEMM (pg_chi0_mixed*, the refinement of
+ * pg_eps_inverse_mixed, pg_selfc_mwm in split precision), for every launch
+ * enqueued after the call; process-wide; 0 restores the default of 5 s.  When
+ * a wait expires the launch sets PG_ERR_TIMEOUT in its status word, leaves
+ * NaN in the tiles it did not finish and returns with its in-flight copies
+ * and MMAs completed, so the context stays usable.  No counterpart in the
+ * reference, whose equivalent failures stop the process
+ * (for_tetrahedra2.f90:1777-1781). */
+void pg_set_wait_limit_ns(unsigned long long ns);
+unsigned long long pg_wait_limit_ns(void);
 
 #ifdef __cplusplus
 }

@@ -26,20 +26,23 @@
 // Kernel layout: a cluster of two CTAs owns a 256×256 block of the upper
 // block triangle of G, per frequency, per K-split.  CTA r of the cluster
 // computes the 128-row tile ti = 2·rp + r against the block's 256 columns
-// (one 128×256 tcgen05.mma per 16 K, or 128×128 on the diagonal); the B-digit
-// tile of the block is loaded half by each CTA and multicast to both, so each
-// SM reads 32 KB from L2 per 64-wide K-block for 2·128·256·64 flop.
+// (one 128×256 tcgen05.mma per 16 K, or 128×128 on the diagonal).  Each CTA
+// loads its own A tile and the whole B-digit tile of the block into its own
+// shared memory (plain TMA loads, no cross-CTA copies); the cluster only makes
+// the two CTAs that read the same B tile run at the same time, so the second
+// read of each B tile is served by L2.
 // Warp 0 issues the TMA loads (A tile + two B halves per stage, 128-byte
 // swizzle, 4 stages), warp 1 allocates TMEM and issues the MMAs, warps 2 …
 // renormalise: the low accumulators (two 256-column TMEM buffers used in
 // turn, so the tensor core keeps working while the previous chunk is
 // renormalised) and a high accumulator per group held in registers (each
 // epilogue thread owns one row × 128 or × 64 columns, see epi_warps).  A stage is refilled only when
-// the MMAs of both CTAs have read it (each MMA commit arrives on both CTAs'
-// "empty" barriers).  Every wait is bounded (≈ 5 s of %globaltimer); on
-// expiry the kernel records PG_ERR_TIMEOUT, drains its own in-flight work,
-// frees TMEM and returns; the cluster's two CTAs meet at a cluster barrier
-// before either exits, so no multicast lands in a finished CTA.
+// this CTA's MMAs have read it (the MMA commit arrives on its "empty" barrier).
+// Every wait is bounded by OzParams::wait_ns of %globaltimer (5 s unless the
+// host sets another limit with pg_set_wait_limit_ns); on expiry the kernel
+// records PG_ERR_TIMEOUT, stops issuing, waits (bounded by a fixed 5 s, never
+// by the shortened limit) until its issued TMA loads have landed and its
+// issued MMAs have completed, frees TMEM and returns.
 #include <cuda_runtime.h>
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -49,6 +52,7 @@
 #include "pygw_status.h"
 #include "launches.h"
 #include "ozaki.h"
+#include "tc_ptx.h"
 
 namespace pgm {
 
@@ -69,7 +73,8 @@ constexpr int STAGE_BYTES = 3 * TILE_BYTES;       // A tile + the two B halves
 __host__ __device__ constexpr int epi_warps(bool general) { return general ? 16 : 8; }
 __host__ __device__ constexpr int gemm_threads(bool general) { return 32 * (2 + epi_warps(general)); }
 constexpr uint32_t TMEM_COLS = 512;               // two 256-column low accumulators
-constexpr unsigned long long WAIT_NS = 5000000000ull;   // 5 s per wait
+constexpr unsigned long long WAIT_NS = 5000000000ull;   // default limit of one wait (5 s)
+constexpr unsigned long long DRAIN_NS = 5000000000ull;  // limit of the drain waits before exit (fixed)
 
 struct OzParams {
   double* out;          // [nsplit][wb][npair][128 (col)][128 (row)]: FP64, or in the general
@@ -82,142 +87,8 @@ struct OzParams {
   int nTb, nTbv, nCb;   // B: 128-row tiles, tiles with real rows, 256-row blocks
   int nw;               // frequencies of this launch (≤ wb, the output's frequency stride)
   int wl0;              // B planes of this launch start at frequency wl0 of the digit array
+  unsigned long long wait_ns;   // limit of one pipeline wait (%globaltimer ns)
 };
-
-// ------------------------------------------------------------ PTX helpers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ unsigned long long gtime() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ uint32_t cluster_rank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ void cluster_sync_all() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait: false (and the abort flag set) if the phase did not complete in WAIT_NS.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, unsigned* status) {
-  if (mbar_test(bar, parity)) return true;
-  const unsigned long long t0 = gtime();
-  while (true) {
-    if (*abort_flag) return false;
-    if (mbar_test(bar, parity)) return true;
-    if (gtime() - t0 > WAIT_NS) {
-      *abort_flag = 1;
-      if (status) atomicOr(status, PG_ERR_TIMEOUT);
-      return false;
-    }
-  }
-}
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::
-          "r"(smem_u32(dst)),
-      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
-      : "memory");
-}
-// The same tile written at this shared-memory offset in every CTA of `mask`,
-// completing bytes on the barrier at the same offset in each of them.
-__device__ __forceinline__ void tma_load_3d_mc(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z,
-                                               uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1, {%3, "
-      "%4, %5}], [%2], %6;" ::"r"(smem_u32(dst)),
-      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z), "h"(mask)
-      : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-// Arrive on the barrier at this offset in every CTA of `mask` once this thread's MMAs have completed.
-__device__ __forceinline__ void tc_commit_mc(uint64_t* bar, uint16_t mask) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::
-                   "r"(smem_u32(bar)),
-               "h"(mask)
-               : "memory");
-}
-__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-          d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
-      : "memory");
-}
-// 32 lanes × 8 consecutive 32-bit columns per warp.
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
-}
-// 32 lanes × 16 consecutive 32-bit columns per warp.
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
-}
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
-  uint32_t r[16];
-#pragma unroll
-  for (int i = 0; i < 16; i++) r[i] = __float_as_uint(v[i]);
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
-          taddr),
-      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
-      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
-      : "memory");
-  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-}
-
-// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle,
-// 8-row core groups 1024 bytes apart (tcgen05 descriptor format, version 1).
-__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);          // start address
-  d |= (uint64_t)1 << 16;                             // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;                   // stride byte offset
-  d |= (uint64_t)1 << 46;                             // descriptor version
-  d |= (uint64_t)2 << 61;                             // 128-byte swizzle
-  return d;
-}
-// Instruction descriptor, kind::f16: D=F32, A=B=BF16, both K-major, M=128, N=n.
-__host__ __device__ constexpr uint32_t idesc_m128(int n) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
-}
 
 // (v.x + v.y) + a + b as a normalised float pair (hi, lo) by Knuth's two-sum:
 // with a, b exact (group integers times 2^-8d) the pair holds the running
@@ -246,11 +117,11 @@ __host__ __device__ __forceinline__ void tri_pair(int lin, int n, int& i, int& j
 }
 
 // Coordinates of load i of a CTA: digit pair (s, t) in the order d = 0..SD−1,
-// s = 0..d, then the K-block; ya / yb = rows of the A tile and of this CTA's
-// half of the B tile, za / zb = their (plane, K-block) slices.
+// s = 0..d, then the K-block; ya / yb = first rows of the A tile and of the
+// block's 256-row B tile, za / zb = their (plane, K-block) slices.
 template <int SD>
 __device__ __forceinline__ void load_coords(const OzParams& p, int i, int nkbs, int kb0, int ti, int wl, int cb,
-                                            int crank, int& ya, int& za, int& yb, int& zb) {
+                                            int& ya, int& za, int& yb, int& zb) {
   const int pi = i / nkbs;
   int d = 0;
   while ((d + 1) * (d + 2) / 2 <= pi) d++;
@@ -258,7 +129,7 @@ __device__ __forceinline__ void load_coords(const OzParams& p, int i, int nkbs, 
   const int kb = kb0 + (i - pi * nkbs);
   ya = ti * TM;
   za = ((p.a_per_w ? wl * SD : 0) + s_) * p.nkb + kb;
-  yb = cb * TN + crank * TM;
+  yb = cb * TN;
   zb = ((p.wl0 + wl) * SD + t_) * p.nkb + kb;
 }
 
@@ -283,7 +154,6 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int crank = (int)cluster_rank();
-  const uint16_t both = (uint16_t)((1u << CL) - 1u);
   // Work units (output block, frequency, K split), numbered with the output
   // block fastest; cluster cid takes units cid, cid + ncl, …  (the host launches
   // one cluster per unit; a smaller grid makes the kernel persistent).
@@ -292,7 +162,7 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
   const int nunits = nitems * p.nw * p.nsplit;
 
   if (threadIdx.x == 0) {
-    for (int i = 0; i < NST; i++) { mbar_init(full + i, 1); mbar_init(empty + i, CL); }
+    for (int i = 0; i < NST; i++) { mbar_init(full + i, 1); mbar_init(empty + i, 1); }
     // acc_empty / group_done: every epilogue thread arrives (no unbounded named barrier)
     for (int i = 0; i < 2; i++) { mbar_init(acc_full + i, 1); mbar_init(acc_empty + i, 32 * NEPI); }
     mbar_init(group_done, 32 * NEPI);
@@ -308,7 +178,7 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
   }
   tc_fence_before();
   __syncthreads();
-  cluster_sync_all();            // the peer's barriers exist before any multicast reaches them
+  cluster_sync_all();            // both CTAs of the cluster start together
   tc_fence_after();
   const uint32_t tmem = *tmem_base_slot;
 
@@ -345,23 +215,25 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
         const int total = (SD * (SD + 1) / 2) * nkbs;
         for (int i = 0; i < total && ok; i++, it++) {
           const int st = it % NST;
-          if (it >= NST) ok = mbar_wait(empty + st, ((it / NST) - 1) & 1, abort_flag, p.status);
+          if (it >= NST) ok = mbar_wait(empty + st, ((it / NST) - 1) & 1, abort_flag, p.status, p.wait_ns);
           if (!ok) break;
           int ya, za, yb, zb;
-          load_coords<SD>(p, i, nkbs, U.kb0, U.ti, U.wl, U.cb, crank, ya, za, yb, zb);
+          load_coords<SD>(p, i, nkbs, U.kb0, U.ti, U.wl, U.cb, ya, za, yb, zb);
           unsigned char* sa = smem + st * STAGE_BYTES;
           mbar_expect_tx(full + st, STAGE_BYTES);
           tma_load_3d(sa, &tmA, full + st, 0, ya, za);
-          tma_load_3d_mc(sa + TILE_BYTES * (1 + crank), &tmB, full + st, 0, yb, zb, both);
+          tma_load_3d(sa + TILE_BYTES, &tmB, full + st, 0, yb, zb);
+          tma_load_3d(sa + 2 * TILE_BYTES, &tmB, full + st, 0, yb + TM, zb);
         }
       }
-      // drain: the last phase of every stage must have been read by both CTAs'
-      // MMAs (so every load and every remote arrival on this CTA has landed)
+      // drain: every issued load has landed before the CTA may exit.  Load j
+      // was issued after the MMAs had read load j − NST (which they waited
+      // for), so only the last NST loads can still be in flight.
       const int issued = it;
       const unsigned long long t0 = gtime();
       for (int j = max(0, issued - NST); j < issued; j++) {
         const int st = j % NST;
-        while (!mbar_test(empty + st, (j / NST) & 1) && gtime() - t0 < WAIT_NS) {}
+        while (!mbar_test(full + st, (j / NST) & 1) && gtime() - t0 < DRAIN_NS) {}
       }
     }
   } else if (warp == 1) {
@@ -375,20 +247,20 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
         const int nchunk_per_pass = (U.kb1 - U.kb0 + LBLK - 1) / LBLK;
         for (int d = 0; d < SD && ok; d++, G++) {
           // the epilogue has combined the previous group (its remainders are read)
-          if (G > 0) ok = mbar_wait(group_done, (G - 1) & 1, abort_flag, p.status);
+          if (G > 0) ok = mbar_wait(group_done, (G - 1) & 1, abort_flag, p.status, p.wait_ns);
           if (!ok) break;
           bool used[2] = {false, false};
           for (int s = 0; s <= d && ok; s++) {
             for (int ch = 0; ch < nchunk_per_pass && ok; ch++, c++) {
               const int b = c & 1;
-              if (c >= 2) ok = mbar_wait(acc_empty + b, ((c >> 1) - 1) & 1, abort_flag, p.status);
+              if (c >= 2) ok = mbar_wait(acc_empty + b, ((c >> 1) - 1) & 1, abort_flag, p.status, p.wait_ns);
               if (!ok) break;
               tc_fence_after();
               const uint32_t dcol = tmem + (uint32_t)(b * TN + U.n_off * TM);
               const int cb0 = U.kb0 + ch * LBLK, cb1 = min(U.kb1, cb0 + LBLK);
               for (int kb = cb0; kb < cb1; kb++, it++) {
                 const int st = it % NST;
-                ok = mbar_wait(full + st, (it / NST) & 1, abort_flag, p.status);
+                ok = mbar_wait(full + st, (it / NST) & 1, abort_flag, p.status, p.wait_ns);
                 if (!ok) break;
                 tc_fence_after();
                 const uint32_t sa = smem_u32(smem + st * STAGE_BYTES);
@@ -398,7 +270,7 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
                   const uint32_t accumulate = (used[b] || kb > cb0 || k > 0) ? 1u : 0u;
                   tc_mma(dcol, ad + (uint64_t)(2 * k), bd + (uint64_t)(2 * k), idesc, accumulate);
                 }
-                tc_commit_mc(empty + st, both);   // stage free in both CTAs once these MMAs have read it
+                tc_commit(empty + st);   // stage free once these MMAs have read it
               }
               if (!ok) break;
               used[b] = true;
@@ -410,7 +282,7 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
       // drain: wait for every MMA this thread issued
       tc_commit(drain);
       const unsigned long long t0 = gtime();
-      while (!mbar_test(drain, 0) && gtime() - t0 < WAIT_NS) {}
+      while (!mbar_test(drain, 0) && gtime() - t0 < DRAIN_NS) {}
     }
   } else {
     // ---------------------------------------------------------- epilogue (warps 2 … 2+NEPI−1)
@@ -439,7 +311,8 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
         const int c_first = c;
         for (int gc = 0; gc < nchunks_group && ok; gc++, c++) {
           const int b = c & 1;
-          ok = mbar_wait(acc_full + b, (c >> 1) & 1, abort_flag, p.status);
+          // warp-uniform outcome: the tcgen05.ld/st below are warp-collective
+          ok = __all_sync(0xffffffffu, mbar_wait(acc_full + b, (c >> 1) & 1, abort_flag, p.status, p.wait_ns));
           if (!ok) break;
           tc_fence_after();
           if (active) {
@@ -838,6 +711,16 @@ using namespace pgm;
 
 static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Limit of one pipeline wait inside k_ozaki_gemm, for every launch after it
+// is set (process-wide; 0 restores the default of 5 s).  A short limit makes
+// a wait expire on purpose: the launch then records PG_ERR_TIMEOUT in its
+// status word, marks its unfinished output tiles with NaN and returns, which
+// is how the expiry path is tested.
+#include <atomic>
+static std::atomic<unsigned long long> g_wait_ns{WAIT_NS};
+extern "C" void pg_set_wait_limit_ns(unsigned long long ns) { g_wait_ns.store(ns ? ns : WAIT_NS); }
+extern "C" unsigned long long pg_wait_limit_ns(void) { return g_wait_ns.load(); }
+
 struct MixedLayout {
   long long K, K_pad;
   int N, R, R_pad, nT, nTv, nC, nitems, npair, nkb, nsplit, kb_per_split, wb, wbp;
@@ -1016,6 +899,7 @@ static int chi0_mixed_impl(const void* minm, int nkp, int k0, const int* kstart,
   op.out = out; op.status = d_status; op.R_pad = L.R_pad; op.nT = L.nT; op.nTv = L.nTv; op.nC = L.nC;
   op.gen = 0; op.a_per_w = 0; op.nTb = L.nT; op.nTbv = L.nTv; op.nCb = L.nC;
   op.npair = L.npair; op.nkb = L.nkb; op.kb_per_split = L.kb_per_split; op.nsplit = L.nsplit; op.wb = wb;
+  op.wait_ns = g_wait_ns.load();
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = CL;
@@ -1128,6 +1012,7 @@ int pgm::launch_gemm_general(const __nv_bfloat16* adig, const __nv_bfloat16* bdi
   op.R_pad = R_padA; op.nT = R_padA / TM; op.nTv = R_padA / TM; op.nC = R_padA / TN;
   op.gen = 1; op.a_per_w = a_per_w ? 1 : 0; op.nTb = R_padB / TM; op.nTbv = nTbv; op.nCb = R_padB / TN;
   op.npair = op.nT * op.nTb; op.nkb = nkb; op.kb_per_split = nkb; op.nsplit = 1; op.wb = nw;
+  op.wait_ns = g_wait_ns.load();
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = CL;

@@ -1331,16 +1331,46 @@ extern "C" int pg_bz_calcqdepw_par3(const double* enk, int nbnd, int nkp, double
 // it has to start at zero, because every call rewrites each entry it reads.
 // All calls share the one array, so calls whose work overlaps on the GPU
 // (different streams, or other threads) race: serialise them.
-// The first call on a device looks up the array's device address (with that
-// device current) and caches it; make that first call before any stream
-// capture.
+// The first call in a device context looks up the array's device address
+// (with that device current) and caches it under the context's unique id, so
+// a new context (after cudaDeviceReset, or another context made current)
+// gets a fresh lookup instead of a stale address; make that first call
+// before any stream capture.
 namespace pgw {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[PG_NOALLOC_SCRATCH_BYTES];
 }
 
 #include <mutex>
+#include <cuda.h>
 static std::mutex g_noalloc_mutex;
 static void* g_noalloc_ptr[64] = {nullptr};
+static unsigned long long g_noalloc_ctx[64] = {0};
+
+// Unique id of the current context (0 if the driver cannot say; the address
+// is then looked up on every call).
+static unsigned long long current_context_id() {
+  typedef CUresult (*get_cur_t)(CUcontext*);
+  typedef CUresult (*get_id_t)(CUcontext, unsigned long long*);
+  static get_cur_t get_cur = nullptr;
+  static get_id_t get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* a = nullptr;
+    void* b = nullptr;
+    cudaDriverEntryPointQueryResult qa, qb;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+        qa == cudaDriverEntryPointSuccess)
+      get_cur = (get_cur_t)a;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+        qb == cudaDriverEntryPointSuccess)
+      get_id = (get_id_t)b;
+    looked_up = true;
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_cur || !get_id || get_cur(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 extern "C" size_t pg_bz_calcqdepw_par2_noalloc_capacity(void) { return (size_t)PG_NOALLOC_SCRATCH_BYTES; }
 
@@ -1358,17 +1388,19 @@ extern "C" int pg_bz_calcqdepw_par2_noalloc(const double* enk, int nbnd, int nkp
   if (lists + per_omega + 256 > (size_t)PG_NOALLOC_SCRATCH_BYTES) return PG_ETOOBIG;
   const size_t fit = ((size_t)PG_NOALLOC_SCRATCH_BYTES - lists - 256) / per_omega;
   const int nomc = (int)((fit < (size_t)nom) ? fit : (size_t)nom);
-  // One-time per-device lookup of the array's device address: in host code
-  // the symbol names a host-side stand-in, not device memory.
+  // Lookup of the array's device address once per device context: in host
+  // code the symbol names a host-side stand-in, not device memory.
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return PG_ECUDA;
   void* base = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_noalloc_ptr[dev] || ctx == 0 || ctx != g_noalloc_ctx[dev]) {
       void* p = nullptr;
       if (cudaGetSymbolAddress(&p, pgw::g_noalloc_scratch) != cudaSuccess || !p) return PG_ECUDA;
       g_noalloc_ptr[dev] = p;
+      g_noalloc_ctx[dev] = ctx;
     }
     base = g_noalloc_ptr[dev];
   }
