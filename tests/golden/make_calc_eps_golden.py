@@ -1,8 +1,8 @@
 """Generate golden vectors for calc_eps from the reference's own code.
 
-Run in a container that holds the reference at /root/reference:
+Run where the reference's source tree is available:
 
-    python tests/golden/make_calc_eps_golden.py
+    python tests/golden/make_calc_eps_golden.py --reference <PyGW source tree>
 
 The reference's driver is Python 2 with f2py modules, so it cannot be
 imported here.  This script reads the text of
@@ -30,9 +30,9 @@ import numpy as np
 import scipy.linalg
 
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
-from refsrc import NS, load  # noqa: E402
+from refsrc import NS, load, reference_file  # noqa: E402
 
-REF = "/root/reference/pygw.py"
+REF = reference_file("pygw.py")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "calc_eps_golden.npz")
 
 

@@ -1,8 +1,8 @@
 """Generate golden vectors for calc_selfc from the reference's own code.
 
-Run in a container that holds the reference at /root/reference:
+Run where the reference's source tree is available:
 
-    python tests/golden/make_calc_selfc_golden.py
+    python tests/golden/make_calc_selfc_golden.py --reference <PyGW source tree>
 
 As make_calc_eps_golden.py does for calc_eps, this reads the text of
 ``MatrixElements2Band.calc_selfc`` (pygw.py:3299-3412) and of
@@ -36,8 +36,8 @@ sys.path.insert(0, HERE)
 import refsrc  # noqa: E402
 from refsrc import NS  # noqa: E402
 
-PYGW = "/root/reference/pygw.py"
-MCOMMON = "/root/reference/mcommon.py"
+PYGW = refsrc.reference_file("pygw.py")
+MCOMMON = refsrc.reference_file("mcommon.py")
 OUT = os.path.join(HERE, "calc_selfc_golden.npz")
 
 

@@ -1,9 +1,9 @@
 """Generate golden vectors for the tetrahedra and the k − q table from the
 reference's own code.
 
-Run in a container that holds the reference at /root/reference:
+Run where the reference's source tree is available:
 
-    python tests/golden/make_mesh_golden.py
+    python tests/golden/make_mesh_golden.py --reference <PyGW source tree>
 
 Runs the text of ``KQmesh.tetra`` (kqmesh.py:188-380) on several meshes and
 reciprocal bases, with its Python branch for the k − q table (``FORT``
@@ -30,7 +30,7 @@ sys.path.insert(0, HERE)
 import refsrc  # noqa: E402
 from refsrc import NS  # noqa: E402
 
-KQMESH = "/root/reference/kqmesh.py"
+KQMESH = refsrc.reference_file("kqmesh.py")
 OUT = os.path.join(HERE, "mesh_golden.npz")
 
 

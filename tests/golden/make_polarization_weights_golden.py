@@ -1,9 +1,9 @@
 """Generate golden vectors for the host side of Polarization_weights from the
 reference's own code.
 
-Run in a container that holds the reference at /root/reference:
+Run where the reference's source tree is available:
 
-    python tests/golden/make_polarization_weights_golden.py
+    python tests/golden/make_polarization_weights_golden.py --reference <PyGW source tree>
 
 Runs the text of ``Polarization_weights`` (pygw.py:3416-3476) with print
 statements rewritten, on seeded band energies with core states and a
@@ -22,9 +22,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
-from refsrc import NS, load  # noqa: E402
+from refsrc import NS, load, reference_file  # noqa: E402
 
-PYGW = "/root/reference/pygw.py"
+PYGW = reference_file("pygw.py")
 OUT = os.path.join(HERE, "polarization_weights_golden.npz")
 
 

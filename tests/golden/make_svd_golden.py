@@ -1,8 +1,8 @@
 """Generate golden vectors for the SVD frequency basis from the reference's own code.
 
-Run in a container that holds the reference at /root/reference:
+Run where the reference's source tree is available:
 
-    python tests/golden/make_svd_golden.py
+    python tests/golden/make_svd_golden.py --reference <PyGW source tree>
 
 Runs the text of ``svd_functions`` (pygw.py:3478-3501) and of
 ``Give2TanMesh`` (mcommon.py:13-31) on two Matsubara meshes.  Two Python 2
@@ -25,8 +25,8 @@ sys.path.insert(0, HERE)
 import refsrc  # noqa: E402
 from refsrc import NS  # noqa: E402
 
-PYGW = "/root/reference/pygw.py"
-MCOMMON = "/root/reference/mcommon.py"
+PYGW = refsrc.reference_file("pygw.py")
+MCOMMON = refsrc.reference_file("mcommon.py")
 OUT = os.path.join(HERE, "svd_golden.npz")
 
 

@@ -8,8 +8,28 @@ code line indented no deeper — and only its Python 2 forms are rewritten:
 dropped first), ``d.has_key(k)`` becomes ``k in d``, and the caller may add
 literal replacements (for a Python 2 integer division).  Nothing else changes.
 """
+import os
 import re
+import sys
 import textwrap
+
+
+def reference_file(name):
+    """Path of ``name`` inside the reference's source tree, whose root is given
+    by ``--reference DIR`` on the command line or the PYGW_REFERENCE
+    environment variable."""
+    root = None
+    if "--reference" in sys.argv:
+        i = sys.argv.index("--reference")
+        if i + 1 < len(sys.argv):
+            root = sys.argv[i + 1]
+    root = root or os.environ.get("PYGW_REFERENCE")
+    if not root:
+        sys.exit("give the reference's source tree: --reference DIR (or PYGW_REFERENCE=DIR)")
+    path = os.path.join(root, name)
+    if not os.path.exists(path):
+        sys.exit(f"{path} not found")
+    return path
 
 
 class NS:
