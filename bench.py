@@ -48,6 +48,9 @@ def parse():
                     help="k-points on which the plain FP64 GPU contraction is timed for the comparison line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="mixed: skip the FP64-vs-mixed eps^-1 comparison on three frequencies (outside the timed "
+                         "region)")
     ap.add_argument("--div", type=int, default=0, help="override the k-mesh divisions (smaller profiling case)")
     ap.add_argument("--npb", type=int, default=0, help="override the product-basis size (smaller profiling case)")
     ap.add_argument("--nom", type=int, default=0, help="override the number of frequencies (smaller profiling case)")
@@ -292,14 +295,79 @@ def bf16_peak():
     return 1700.0, "of fallback (sustained)"
 
 
-# DRAM bytes (read + written) of one k_ozaki_gemm launch of the χ0 digit GEMM,
-# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one capture)
-# per launch shape: (workload, N_PB, k-points, frequencies per launch).
-MEASURED_GEMM_TRAFFIC = {
-    ("C3", 1200, 216, 1): 426.53e9 + 0.65e9,
-    ("C3", 1200, 216, 2): 1050.0e9 + 1.83e9,
-    ("C3", 1200, 216, 4): 2280.0e9 + 3.79e9,
-}
+# DRAM bytes (read + written) of one launch of the χ0 digit GEMM, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) per kernel build and
+# launch shape: (kernel, workload, N_PB, k-points, frequencies per launch) ->
+# (bytes, where the capture is summarised).  A launch whose kernel or shape has
+# no entry reports traffic null and says so.
+MEASURED_GEMM_TRAFFIC = {}
+
+
+# FP64 work of the weights kernel and the FP64 ceiling it is held to, from one
+# ncu capture of k_tet_weights and k_chi0_f64 (thread-level dadd + dmul + 2·dfma
+# instruction counts, gpu__time_duration): (FP64 flops of k_tet_weights per
+# (sub-tetrahedron, ω) evaluation — geometry included — counted by its exact +
+# Taylor counters; k_chi0_f64's FP64 rate in TFLOP/s, the FP64 pipe then being
+# nearly saturated; where the capture is summarised).
+WEIGHTS_FP64 = (614.8, 1.212, "profiles/fp64_work_k_tet_weights_k_chi0_f64_c2_div4.md")
+
+
+def measure_accuracy(inp):
+    """Split-precision ε⁻¹ of the benchmarked q against the FP64 GPU path, on
+    the lowest, a middle and the highest frequency, with every k-point
+    (outside the timed region)."""
+    from pygw_gb300 import accuracy
+    from pygw_gb300 import polarization as pol
+    iq = inp.qs[0]
+    r = pol.weights_device(inp.enk_d, inp.ef, inp.kqid_d[iq], 0, inp.nomx, inp.numin, inp.om_d, inp.tetc_d)
+    nom = inp.w.nom
+    t0 = time.perf_counter()
+    acc = accuracy.mixed_vs_fp64(r.kcw, inp.minm_dev, inp.nkp, inp.w.npb, inp.nb1, inp.nb2,
+                                 sorted({0, nom // 2, nom - 1}))
+    acc["seconds"] = time.perf_counter() - t0
+    acc["note"] = ("eps^-1 of the benchmarked q from the split-precision path vs the FP64 GPU path, same weights and "
+                   "matrix elements, all k-points; normwise = max|d|/max|ref| (the 1e-9 bar), elementwise = "
+                   "max|d_ij|/|ref_ij| over |ref_ij| > elementwise_floor*max|ref|")
+    return acc
+
+
+def weights_roofline(inp):
+    """Roofline of the weights phase of one q (the first): the kcw bytes it
+    writes against the HBM copy bandwidth, and its FP64 work (from the
+    kernel's own evaluation counters) against the FP64 ceiling of the plain
+    FP64 contraction.  Timed with CUDA events around the phase (warm)."""
+    import torch
+    from pygw_gb300 import polarization as pol
+    iq = inp.qs[0]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ts = []
+    for _ in range(3):
+        ev[0].record()
+        r = pol.weights_device(inp.enk_d, inp.ef, inp.kqid_d[iq], 0, inp.nomx, inp.numin, inp.om_d, inp.tetc_d)
+        ev[1].record()
+        torch.cuda.synchronize()
+        ts.append(ev[0].elapsed_time(ev[1]))
+    t_ms = statistics.median(ts)
+    c = r.counters
+    nom = inp.w.nom
+    kcw_bytes = 8 * inp.nb1 * inp.nb2 * inp.nkp * nom
+    hbm = json.load(open(PEAKS_FILE)).get("hbm_gbs") if os.path.exists(PEAKS_FILE) else 6800.0
+    gbs = kcw_bytes / (t_ms * 1e-3) / 1e9
+    out = {"kernel": "weights phase (k_tet_classify, k_class_scatter, k_tet_weights, k_gather, k lists)",
+           "phase_ms": t_ms, "evaluations": {"exact": c["exact"], "taylor": c["taylor"], "calls": c["calls"]},
+           "hbm": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                   "algorithmic_bytes": kcw_bytes, "note": "kcw written (8 B per band pair, k-point, frequency) / "
+                                                          "phase time; peak = measured copy bandwidth"},
+           "fp64": None}
+    if WEIGHTS_FP64 is not None:
+        per_eval, ceiling, src = WEIGHTS_FP64
+        flops = per_eval * (c["exact"] + c["taylor"])
+        tf = flops / (t_ms * 1e-3) / 1e12
+        out["fp64"] = {"bound": "fp64", "achieved": tf, "peak": ceiling, "unit": "TFLOP/s", "frac": tf / ceiling,
+                       "flops": flops, "source": src,
+                       "note": "FP64 flops = per-evaluation count x (exact + Taylor evaluations of this q); "
+                               "peak = FP64 rate of this build's k_chi0_f64 (FP64 pipe near saturation)"}
+    return out
 
 
 # GB300's FP64 rate (CUDA cores; it has no faster FP64 tensor path).  The
@@ -352,7 +420,8 @@ def cpu_sample_seconds_per_q(w, nk_sample=2, nom_sample=8, threads=0):
     desc = (f"oracle C++ weights on {len(osel)}/{len(om)} frequencies ({os.cpu_count()} threads) scaled: {t_w:.2f}s; "
             f"numpy contraction on {len(ks)}/{nkp} k-points, all frequencies, scaled: {t_c:.2f}s; numpy inverse "
             f"on {len(osel)}/{len(om)} frequencies scaled: {t_i:.2f}s")
-    return t_w + t_c + t_i, desc
+    measured = {"weights": len(osel) / len(om), "contraction": len(ks) / nkp, "inverse": len(osel) / len(om)}
+    return t_w + t_c + t_i, desc, measured
 
 
 def run_reference(a, w, rank):
@@ -361,9 +430,9 @@ def run_reference(a, w, rank):
     from oracle.build import build as build_oracle
     build_oracle()
     cpu_sample_seconds_per_q(w, nk_sample=2)      # warm caches/threads (outside timing)
-    times, desc = [], ""
+    times, desc, measured = [], "", {}
     for i in range(a.warmup + a.steps):
-        t, desc = cpu_sample_seconds_per_q(w)
+        t, desc, measured = cpu_sample_seconds_per_q(w)
         if i >= a.warmup:
             times.append(t)
     v = max(times)
@@ -373,7 +442,11 @@ def run_reference(a, w, rank):
             "impl": "reference",
             "config": {"workload": workload_desc(w), "precision": "fp64", "parallelism": "replicas"},
             "cpu_baseline": {"value": v, "unit": "s/q-point", "cores": os.cpu_count(), "kind": "port",
-                             "sample": desc},
+                             "sample": desc, "extrapolated": True, "measured_fraction": measured},
+            "extrapolated": True,
+            "extrapolation": ("each step times a bounded sample of the q-point (fractions in "
+                              "cpu_baseline.measured_fraction, each part linear in what it samples) and scales it to "
+                              "the whole q-point, so value and ms_per_step are modelled, not a wall-clock step"),
             "e2e": {"value": v, "unit": "s/q-point", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -797,10 +870,12 @@ def main():
         # distinct digit bytes of one launch: the A planes once, the B planes of each frequency
         rpad = -(-2 * npb // 256) * 256
         dig_bytes = 5 * rpad * kpad * 2 * (1 + inp.wb)
-        traffic = MEASURED_GEMM_TRAFFIC.get((w.name, npb, inp.nkp, inp.wb))
+        tkey = ("k_ozaki_gemm", w.name, npb, inp.nkp, inp.wb)
+        traffic, traffic_src = MEASURED_GEMM_TRAFFIC.get(tkey, (None, None))
         hbm = json.load(open(PEAKS_FILE)).get("hbm_gbs") if os.path.exists(PEAKS_FILE) else None
         roof = {"kernel": "k_ozaki_gemm", "bound": "tensor", "achieved": alg / g_s / 1e12,
                 "peak": peak, "unit": "TFLOP/s", "frac": alg / g_s / 1e12 / peak, "traffic": traffic,
+                "traffic_source": traffic_src or f"no ncu capture of this kernel build at this launch shape {tkey}",
                 "algorithmic_bytes": dig_bytes,
                 "dram_frac": (traffic / (g_s / len(g_ms)) / 1e9 / hbm) if traffic and hbm else None,
                 "launches": len(g_ms), "ms_per_launch": sum(g_ms) / max(1, len(g_ms)),
@@ -810,7 +885,8 @@ def main():
                 "note": "achieved = 8*N_PB^2*P*Nk*Nw per launch (the reference's complex FP64 GEMM count) / "
                         "CUDA-event launch time of k_ozaki_gemm; executed_bf16 = 15 digit-pair bf16 products "
                         "over the computed 128x256 / 128x128 tiles; peak = bf16 " + peak_note + "; traffic = "
-                        "DRAM bytes per launch from one ncu capture of this launch shape (null if not captured), "
+                        "DRAM bytes per launch from one ncu capture of this kernel build and launch shape "
+                        "(traffic_source; null if not captured), "
                         "algorithmic_bytes = the distinct digit planes the launch reads, dram_frac = traffic / "
                         "launch time / measured HBM copy bandwidth"}
     else:
@@ -826,6 +902,10 @@ def main():
     if a.precision == "mixed" and a.fp64_k_sample > 0:
         v64, parts = fp64_gpu_estimate(inp, a.fp64_k_sample)
         fp64 = {"value": v64, "unit": "s/q-point", **parts}
+    roof_w = weights_roofline(inp)
+    acc = None
+    if a.precision == "mixed" and not a.no_accuracy:
+        acc = measure_accuracy(inp)
 
     e2e = None
     if not a.no_e2e:
@@ -855,8 +935,9 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
-        v, desc = cpu_sample_seconds_per_q(w)
-        cpu = {"value": v, "unit": "s/q-point", "cores": os.cpu_count(), "kind": "port", "sample": desc}
+        v, desc, measured = cpu_sample_seconds_per_q(w)
+        cpu = {"value": v, "unit": "s/q-point", "cores": os.cpu_count(), "kind": "port", "sample": desc,
+               "extrapolated": True, "measured_fraction": measured}
 
     torch.cuda.synchronize()
     sampler.stop()
@@ -871,8 +952,9 @@ def main():
                 "config": {"workload": workload_desc(w), "precision": a.precision, "parallelism": "replicas",
                            "l2": "inputs larger than L2 (matrix elements %.2f GB read every step)"
                                  % (inp.minm_host.numel() * 16 / 1e9)},
-                "roofline": roof, "kernel_status": status_bits, "phases_ms": phase_ms, "fp64_gpu": fp64,
-                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks}
+                "roofline": roof, "roofline_weights": roof_w, "accuracy": acc, "kernel_status": status_bits,
+                "phases_ms": phase_ms, "fp64_gpu": fp64, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": int(launches), "clocks": clocks}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
