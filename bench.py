@@ -268,20 +268,11 @@ def e2e_step(inp, step, out_host, precision="fp64"):
 
 
 def mixed_tile_area(npb):
-    """Output elements the digit GEMM computes per frequency and K (the tile
-    schedule of k_ozaki_gemm: 256x256 blocks of the upper block triangle, each
-    CTA 128 rows x 128 or 256 columns)."""
-    R = 2 * npb
-    rpad = -(-R // 256) * 256
-    ntv, nc = -(-R // 128), rpad // 256
-    area = 0
-    for rp in range(nc):
-        for cb in range(rp, nc):
-            for r in range(2):
-                ti = 2 * rp + r
-                n_off = 1 if ti > 2 * cb else 0
-                area += 128 * 128 * max(1, min(2 * cb + 2, ntv) - (2 * cb + n_off))
-    return area
+    """Output elements the digit GEMM computes per frequency and K: 256x256
+    blocks of the upper block triangle of the 2N x 2N product (k_ozaki_gemm,
+    one 2-SM MMA per block and 16 K)."""
+    nc = -(-2 * npb // 256)
+    return nc * (nc + 1) // 2 * 256 * 256
 
 
 def bf16_peak():
@@ -884,7 +875,7 @@ def main():
                 "chi0_phase_algorithmic_tflops": achieved,
                 "note": "achieved = 8*N_PB^2*P*Nk*Nw per launch (the reference's complex FP64 GEMM count) / "
                         "CUDA-event launch time of k_ozaki_gemm; executed_bf16 = 15 digit-pair bf16 products "
-                        "over the computed 128x256 / 128x128 tiles; peak = bf16 " + peak_note + "; traffic = "
+                        "over the computed 256x256 blocks; peak = bf16 " + peak_note + "; traffic = "
                         "DRAM bytes per launch from one ncu capture of this kernel build and launch shape "
                         "(traffic_source; null if not captured), "
                         "algorithmic_bytes = the distinct digit planes the launch reads, dram_frac = traffic / "

@@ -23,21 +23,24 @@
 // rounding is the dropped 5th-digit residual and the dropped d ≥ 5 pairs
 // (≈ 1e-11 relative per row scale).
 //
-// Kernel layout: a cluster of two CTAs owns a 256×256 block of the upper
-// block triangle of G, per frequency, per K-split.  CTA r of the cluster
-// computes the 128-row tile ti = 2·rp + r against the block's 256 columns
-// (one 128×256 tcgen05.mma per 16 K, or 128×128 on the diagonal).  Each CTA
-// loads its own A tile and the whole B-digit tile of the block into its own
-// shared memory (plain TMA loads, no cross-CTA copies); the cluster only makes
-// the two CTAs that read the same B tile run at the same time, so the second
-// read of each B tile is served by L2.
-// Warp 0 issues the TMA loads (A tile + two B halves per stage, 128-byte
-// swizzle, 4 stages), warp 1 allocates TMEM and issues the MMAs, warps 2 …
+// Kernel layout: a cluster of two CTAs (a CTA pair) owns a 256×256 block of
+// the upper block triangle of G, per frequency, per K-split, computed by
+// 2-SM MMAs (tcgen05.mma.cta_group::2, M = 256, N = 256, K = 16) that the
+// pair's first CTA issues: CTA r holds the 128 A rows of tile ti = 2·rp + r
+// and the 128 B rows cb·256 + r·128 … of the block in its own shared memory
+// (plain TMA loads into its own shared memory, completing on the first CTA's
+// barrier), and its 128 rows × 256 columns of the accumulator in its own
+// tensor memory.  Each SM thus reads 32 KB from L2 per 64-wide K-block, and a
+// stage is 32 KB, so six stages fit.
+// Warp 0 issues the TMA loads (A tile + the CTA's B half per stage, 128-byte
+// swizzle, 6 stages), warp 1 allocates TMEM and (first CTA) issues the MMAs, warps 2 …
 // renormalise: the low accumulators (two 256-column TMEM buffers used in
 // turn, so the tensor core keeps working while the previous chunk is
 // renormalised) and a high accumulator per group held in registers (each
 // epilogue thread owns one row × 128 or × 64 columns, see epi_warps).  A stage is refilled only when
-// this CTA's MMAs have read it (the MMA commit arrives on its "empty" barrier).
+// the pair's MMAs have read it (each MMA commit arrives on both CTAs' "empty"
+// barriers); the MMA issuer reuses an accumulator when the epilogue threads
+// of both CTAs have arrived on its barrier.
 // Every wait is bounded by OzParams::wait_ns of %globaltimer (5 s unless the
 // host sets another limit with pg_set_wait_limit_ns); on expiry the kernel
 // records PG_ERR_TIMEOUT, stops issuing, waits (bounded by a fixed 5 s, never
@@ -60,11 +63,11 @@ constexpr int S = OZ_S;         // digits per value
 constexpr int TM = 128;         // tile rows (A) = B rows loaded by one CTA
 constexpr int TN = 256;         // columns of a cluster's block
 constexpr int KB = 64;          // K per stage (one 128-byte swizzle row of bf16)
-constexpr int NST = 4;          // pipeline stages
+constexpr int NST = 6;          // pipeline stages
 constexpr int LBLK = 14;        // K-blocks per exact chunk: 14·64·129² + 2^11 < 2^24
-constexpr int CL = 2;           // CTAs per cluster (share the B tile)
+constexpr int CL = 2;           // CTAs per cluster: the pair of a 2-SM MMA
 constexpr int TILE_BYTES = TM * KB * 2;           // 16 KB: one 128-row digit tile
-constexpr int STAGE_BYTES = 3 * TILE_BYTES;       // A tile + the two B halves
+constexpr int STAGE_BYTES = 2 * TILE_BYTES;       // A tile + this CTA's B half
 // Epilogue warps: 8 (each thread one row × 128 columns) for the symmetric χ0
 // product, whose long K hides the epilogue behind the MMAs; 16 (one row × 64
 // columns) for the general product, whose short K leaves the digit-group ends
@@ -89,6 +92,56 @@ struct OzParams {
   int wl0;              // B planes of this launch start at frequency wl0 of the digit array
   unsigned long long wait_ns;   // limit of one pipeline wait (%globaltimer ns)
 };
+
+// ------------------------------------------------ 2-SM (CTA pair) helpers
+// Shared::cluster address of this CTA's shared variable at `a` in CTA `rank`.
+__device__ __forceinline__ uint32_t mapa_rank(uint32_t a, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+// Arrive on an mbarrier given by its shared::cluster address (either CTA of the pair).
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster) : "memory");
+}
+// TMA tile load into this CTA's shared memory, completing on the barrier at
+// shared::cluster address bar_cluster (which may be the pair's other CTA's).
+__device__ __forceinline__ void tma_load_3d_pair(void* dst, const CUtensorMap* map, uint32_t bar_cluster, int x,
+                                                 int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, "
+      "%5}], [%2];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(bar_cluster), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+// 2-SM MMA: D (both CTAs' tensor memory, 128 lanes each) += A (128 rows from
+// each CTA) · B (N/2 rows from each CTA), operands at the same shared-memory
+// offsets in both CTAs.
+__device__ __forceinline__ void tc_mma_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+      : "memory");
+}
+// Arrive on the barrier at this shared-memory offset in both CTAs of the pair
+// once the pair's MMAs issued so far by this thread have completed.
+__device__ __forceinline__ void tc_commit_pair(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::
+                   "r"(smem_u32(bar)),
+               "h"((uint16_t)3)
+               : "memory");
+}
+// The same, on this CTA's barrier only.
+__device__ __forceinline__ void tc_commit_pair_local(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+// Instruction descriptor, kind::f16: D=F32, A=B=BF16, both K-major, M=256 (pair), N=n.
+__host__ __device__ constexpr uint32_t idesc_m256(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+}
 
 // (v.x + v.y) + a + b as a normalised float pair (hi, lo) by Knuth's two-sum:
 // with a, b exact (group integers times 2^-8d) the pair holds the running
@@ -117,11 +170,11 @@ __host__ __device__ __forceinline__ void tri_pair(int lin, int n, int& i, int& j
 }
 
 // Coordinates of load i of a CTA: digit pair (s, t) in the order d = 0..SD−1,
-// s = 0..d, then the K-block; ya / yb = first rows of the A tile and of the
-// block's 256-row B tile, za / zb = their (plane, K-block) slices.
+// s = 0..d, then the K-block; ya / yb = first rows of the A tile and of this
+// CTA's 128-row half of the block's B tile, za / zb = their (plane, K-block) slices.
 template <int SD>
 __device__ __forceinline__ void load_coords(const OzParams& p, int i, int nkbs, int kb0, int ti, int wl, int cb,
-                                            int& ya, int& za, int& yb, int& zb) {
+                                            int crank, int& ya, int& za, int& yb, int& zb) {
   const int pi = i / nkbs;
   int d = 0;
   while ((d + 1) * (d + 2) / 2 <= pi) d++;
@@ -129,7 +182,7 @@ __device__ __forceinline__ void load_coords(const OzParams& p, int i, int nkbs, 
   const int kb = kb0 + (i - pi * nkbs);
   ya = ti * TM;
   za = ((p.a_per_w ? wl * SD : 0) + s_) * p.nkb + kb;
-  yb = cb * TN;
+  yb = cb * TN + crank * TM;
   zb = ((p.wl0 + wl) * SD + t_) * p.nkb + kb;
 }
 
@@ -164,27 +217,30 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
   if (threadIdx.x == 0) {
     for (int i = 0; i < NST; i++) { mbar_init(full + i, 1); mbar_init(empty + i, 1); }
     // acc_empty / group_done: every epilogue thread arrives (no unbounded named barrier)
-    for (int i = 0; i < 2; i++) { mbar_init(acc_full + i, 1); mbar_init(acc_empty + i, 32 * NEPI); }
-    mbar_init(group_done, 32 * NEPI);
+    // (the first CTA's acc_empty / group_done take the epilogue threads of both CTAs)
+    for (int i = 0; i < 2; i++) { mbar_init(acc_full + i, 1); mbar_init(acc_empty + i, CL * 32 * NEPI); }
+    mbar_init(group_done, CL * 32 * NEPI);
     mbar_init(drain, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_base_slot)),
+    // one warp of each CTA of the pair allocates, together
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_base_slot)),
                  "r"(TMEM_COLS)
                  : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
   }
   tc_fence_before();
   __syncthreads();
-  cluster_sync_all();            // both CTAs of the cluster start together
+  cluster_sync_all();            // the pair's barriers exist before either CTA signals the other's
   tc_fence_after();
   const uint32_t tmem = *tmem_base_slot;
 
-  // One unit: output block (rp, cb), this CTA's row tile ti, the kept column
-  // tiles (n_off, n_tiles), frequency wl and K range [kb0, kb1).
-  struct Unit { int rp, cb, ti, n_off, n_tiles, wl, split, kb0, kb1; };
+  // One unit: output block (rp, cb), this CTA's row tile ti, frequency wl and
+  // K range [kb0, kb1); the pair's MMA computes both 128-column tiles of the
+  // block (the one below the diagonal of a diagonal block is not stored).
+  struct Unit { int rp, cb, ti, wl, split, kb0, kb1; };
   auto unit = [&](int u) {
     Unit U;
     const int item = u % nitems, rest = u / nitems;
@@ -193,11 +249,6 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
     if (p.gen) { U.rp = item / p.nCb; U.cb = item % p.nCb; }
     else tri_pair(item, p.nC, U.rp, U.cb);
     U.ti = 2 * U.rp + crank;
-    // column tiles 2cb, 2cb+1 that are kept (upper triangle of the symmetric
-    // product) and hold real rows (at least one, so both CTAs issue MMAs)
-    U.n_off = (!p.gen && U.ti > 2 * U.cb) ? 1 : 0;
-    U.n_tiles = min(2 * U.cb + 2, p.nTbv) - (2 * U.cb + U.n_off);
-    if (U.n_tiles < 1) U.n_tiles = 1;
     U.kb0 = U.split * p.kb_per_split;
     U.kb1 = min(p.nkb, U.kb0 + p.kb_per_split);
     return U;
@@ -218,32 +269,33 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
           if (it >= NST) ok = mbar_wait(empty + st, ((it / NST) - 1) & 1, abort_flag, p.status, p.wait_ns);
           if (!ok) break;
           int ya, za, yb, zb;
-          load_coords<SD>(p, i, nkbs, U.kb0, U.ti, U.wl, U.cb, ya, za, yb, zb);
+          load_coords<SD>(p, i, nkbs, U.kb0, U.ti, U.wl, U.cb, crank, ya, za, yb, zb);
           unsigned char* sa = smem + st * STAGE_BYTES;
-          mbar_expect_tx(full + st, STAGE_BYTES);
-          tma_load_3d(sa, &tmA, full + st, 0, ya, za);
-          tma_load_3d(sa + TILE_BYTES, &tmB, full + st, 0, yb, zb);
-          tma_load_3d(sa + 2 * TILE_BYTES, &tmB, full + st, 0, yb + TM, zb);
+          // both CTAs' loads of this stage complete on the first CTA's barrier,
+          // which expects the bytes of both
+          if (crank == 0) mbar_expect_tx(full + st, CL * STAGE_BYTES);
+          const uint32_t bar = mapa_rank(smem_u32(full + st), 0);
+          tma_load_3d_pair(sa, &tmA, bar, 0, ya, za);
+          tma_load_3d_pair(sa + TILE_BYTES, &tmB, bar, 0, yb, zb);
         }
       }
-      // drain: every issued load has landed before the CTA may exit.  Load j
-      // was issued after the MMAs had read load j − NST (which they waited
-      // for), so only the last NST loads can still be in flight.
+      // drain: the last phase of every stage has been read by the pair's MMAs
+      // (so every load into this CTA has landed) before the CTA may exit
       const int issued = it;
       const unsigned long long t0 = gtime();
       for (int j = max(0, issued - NST); j < issued; j++) {
         const int st = j % NST;
-        while (!mbar_test(full + st, (j / NST) & 1) && gtime() - t0 < DRAIN_NS) {}
+        while (!mbar_test(empty + st, (j / NST) & 1) && gtime() - t0 < DRAIN_NS) {}
       }
     }
   } else if (warp == 1) {
-    // ---------------------------------------------------------- MMA issuer
-    if (lane == 0) {
+    // ---------------------------------------------------------- MMA issuer (first CTA of the pair)
+    if (lane == 0 && crank == 0) {
       int it = 0, c = 0, G = 0;          // loads, chunks and digit groups consumed so far
       bool ok = true;
+      const uint32_t idesc = idesc_m256(TN);
       for (int u = cid; u < nunits && ok; u += ncl) {
         const Unit U = unit(u);
-        const uint32_t idesc = idesc_m128(TM * U.n_tiles);
         const int nchunk_per_pass = (U.kb1 - U.kb0 + LBLK - 1) / LBLK;
         for (int d = 0; d < SD && ok; d++, G++) {
           // the epilogue has combined the previous group (its remainders are read)
@@ -256,7 +308,7 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
               if (c >= 2) ok = mbar_wait(acc_empty + b, ((c >> 1) - 1) & 1, abort_flag, p.status, p.wait_ns);
               if (!ok) break;
               tc_fence_after();
-              const uint32_t dcol = tmem + (uint32_t)(b * TN + U.n_off * TM);
+              const uint32_t dcol = tmem + (uint32_t)(b * TN);
               const int cb0 = U.kb0 + ch * LBLK, cb1 = min(U.kb1, cb0 + LBLK);
               for (int kb = cb0; kb < cb1; kb++, it++) {
                 const int st = it % NST;
@@ -264,23 +316,23 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
                 if (!ok) break;
                 tc_fence_after();
                 const uint32_t sa = smem_u32(smem + st * STAGE_BYTES);
-                const uint64_t ad = sdesc_sw128(sa), bd = sdesc_sw128(sa + TILE_BYTES * (1 + U.n_off));
+                const uint64_t ad = sdesc_sw128(sa), bd = sdesc_sw128(sa + TILE_BYTES);
 #pragma unroll
                 for (int k = 0; k < KB / 16; k++) {
                   const uint32_t accumulate = (used[b] || kb > cb0 || k > 0) ? 1u : 0u;
-                  tc_mma(dcol, ad + (uint64_t)(2 * k), bd + (uint64_t)(2 * k), idesc, accumulate);
+                  tc_mma_pair(dcol, ad + (uint64_t)(2 * k), bd + (uint64_t)(2 * k), idesc, accumulate);
                 }
-                tc_commit(empty + st);   // stage free once these MMAs have read it
+                tc_commit_pair(empty + st);   // stage free in both CTAs once these MMAs have read it
               }
               if (!ok) break;
               used[b] = true;
-              tc_commit(acc_full + b);     // chunk complete
+              tc_commit_pair(acc_full + b);     // chunk complete in both CTAs' tensor memory
             }
           }
         }
       }
       // drain: wait for every MMA this thread issued
-      tc_commit(drain);
+      tc_commit_pair_local(drain);
       const unsigned long long t0 = gtime();
       while (!mbar_test(drain, 0) && gtime() - t0 < DRAIN_NS) {}
     }
@@ -299,8 +351,10 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
     for (int u = cid; u < nunits && ok; u += ncl) {
       const Unit U = unit(u);
       const int tj = 2 * U.cb + h;
-      const bool active = h >= U.n_off && h < U.n_off + U.n_tiles;
       const bool stored = p.gen || tj >= U.ti;     // tile (ti, tj) is kept
+      // a tile below the diagonal is computed by the pair's MMA but neither
+      // read nor stored (its accumulator columns are left to grow)
+      const bool active = stored;
       const int pair = p.gen ? U.ti * p.nTb + tj : stored ? U.ti * p.nT - U.ti * (U.ti - 1) / 2 + (tj - U.ti) : 0;
       double* out = p.out + ((((size_t)U.split * p.wb + U.wl) * p.npair + pair) * TM) * TM;
       const int nchunk_per_pass = (U.kb1 - U.kb0 + LBLK - 1) / LBLK;
@@ -371,13 +425,12 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
             }
           }
           tc_fence_before();
-          mbar_arrive(acc_empty + b);
-          if (gc == nchunks_group - 1) mbar_arrive(group_done);
+          // the MMA issuer (first CTA) waits for the epilogue threads of both CTAs
+          mbar_arrive_cluster(mapa_rank(smem_u32(acc_empty + b), 0));
+          if (gc == nchunks_group - 1) mbar_arrive_cluster(mapa_rank(smem_u32(group_done), 0));
         }
       }
-      if (stored && !active) {
-        for (int i = 0; i < CW; i++) out[(size_t)(co + i) * TM + row] = 0.0;        // padding tile
-      } else if (stored && !ok) {
+      if (stored && !ok) {
         for (int i = 0; i < CW; i++) out[(size_t)(co + i) * TM + row] = __longlong_as_double(0x7ff8dead00000000LL);
       }
     }
@@ -387,7 +440,7 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
   cluster_sync_all();            // neither CTA leaves while the other may still write to it
   tc_fence_after();
   if (warp == 1) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
 }
 
