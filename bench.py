@@ -291,7 +291,10 @@ def bf16_peak():
 # launch shape: (kernel, workload, N_PB, k-points, frequencies per launch) ->
 # (bytes, where the capture is summarised).  A launch whose kernel or shape has
 # no entry reports traffic null and says so.
-MEASURED_GEMM_TRAFFIC = {}
+GEMM_BUILD = "k_ozaki_gemm 2-SM M256 N256, 6 stages"
+MEASURED_GEMM_TRAFFIC = {
+    (GEMM_BUILD, "C3", 1200, 216, 1): (287.65e9 + 0.59e9, "profiles/k_ozaki_gemm_2sm_c3_dram_traffic.md"),
+}
 
 
 # FP64 work of the weights kernel and the FP64 ceiling it is held to, from one
@@ -861,7 +864,7 @@ def main():
         # distinct digit bytes of one launch: the A planes once, the B planes of each frequency
         rpad = -(-2 * npb // 256) * 256
         dig_bytes = 5 * rpad * kpad * 2 * (1 + inp.wb)
-        tkey = ("k_ozaki_gemm", w.name, npb, inp.nkp, inp.wb)
+        tkey = (GEMM_BUILD, w.name, npb, inp.nkp, inp.wb)
         traffic, traffic_src = MEASURED_GEMM_TRAFFIC.get(tkey, (None, None))
         hbm = json.load(open(PEAKS_FILE)).get("hbm_gbs") if os.path.exists(PEAKS_FILE) else None
         roof = {"kernel": "k_ozaki_gemm", "bound": "tensor", "achieved": alg / g_s / 1e12,
