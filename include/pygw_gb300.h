@@ -231,6 +231,18 @@ unsigned long long pg_launch_count(void);
 void pg_set_wait_limit_ns(unsigned long long ns);
 unsigned long long pg_wait_limit_ns(void);
 
+/* Frequencies whose B digit planes pg_chi0_mixed* prepares per pass over the
+ * A digit planes (process-wide; read by every workspace query and call after
+ * it is set, so set it before sizing a workspace).  A pass reads the five A
+ * planes once and writes five B planes per frequency: a longer pass reads
+ * less per frequency and needs one more set of B planes of workspace per
+ * frequency.  The pass is rounded up to a whole number of omega_batch
+ * launches.  n in [0, 64]; 0 restores the default, 4; returns PG_EARG
+ * otherwise.  No counterpart in the reference (an implementation detail of
+ * the split-precision contraction). */
+int pg_set_chi0_prep_batch(int n);
+int pg_chi0_prep_batch(void);
+
 #ifdef __cplusplus
 }
 #endif

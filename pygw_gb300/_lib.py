@@ -61,6 +61,8 @@ SIGNATURES = {
     "pg_launch_count": (ctypes.c_ulonglong, []),
     "pg_set_wait_limit_ns": (None, [ctypes.c_ulonglong]),
     "pg_wait_limit_ns": (ctypes.c_ulonglong, []),
+    "pg_set_chi0_prep_batch": (c_int, [c_int]),
+    "pg_chi0_prep_batch": (c_int, []),
     "pg_eps_inverse_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                                    c_void_p]),
 }

@@ -216,10 +216,10 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < NST; i++) { mbar_init(full + i, 1); mbar_init(empty + i, 1); }
-    // acc_empty / group_done: every epilogue thread arrives (no unbounded named barrier)
-    // (the first CTA's acc_empty / group_done take the epilogue threads of both CTAs)
-    for (int i = 0; i < 2; i++) { mbar_init(acc_full + i, 1); mbar_init(acc_empty + i, CL * 32 * NEPI); }
-    mbar_init(group_done, CL * 32 * NEPI);
+    // acc_empty / group_done: one arrival per epilogue warp (no unbounded named
+    // barrier); the first CTA's barriers take the epilogue warps of both CTAs
+    for (int i = 0; i < 2; i++) { mbar_init(acc_full + i, 1); mbar_init(acc_empty + i, CL * NEPI); }
+    mbar_init(group_done, CL * NEPI);
     mbar_init(drain, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -377,8 +377,12 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
               tmem_ld16(tl + cc * 16, lo);
 #pragma unroll
               for (int i = 0; i < 16; i++) {
-                const float hh = rintf(lo[i] * (1.0f / 4096.0f)) * 4096.0f;   // multiple of 2^12
-                lo[i] = lo[i] - hh;                                            // |residual| ≤ 2^11
+                // nearest multiple of 2^12 (ties to even): lo + 1.5·2^35 lies in
+                // [2^35, 2^36), where the float spacing is 2^12 (|lo| < 2^24), so
+                // the addition rounds lo there and the subtraction is exact — two
+                // additions instead of a multiply, a rounding and a multiply
+                const float hh = __fsub_rn(__fadd_rn(lo[i], 0x1.8p35f), 0x1.8p35f);
+                lo[i] = __fsub_rn(lo[i], hh);                                  // |residual| ≤ 2^11
                 hi[cc * 16 + i] += hh;
               }
               tmem_st16(tl + cc * 16, lo);
@@ -424,10 +428,15 @@ __global__ void __launch_bounds__(gemm_threads(DF), 1)
               }
             }
           }
+          // the MMA issuer (first CTA) waits for the epilogue warps of both CTAs:
+          // each thread's tensor-memory accesses are complete (waited above) and
+          // fenced, the warp converges, and one lane arrives for all 32
           tc_fence_before();
-          // the MMA issuer (first CTA) waits for the epilogue threads of both CTAs
-          mbar_arrive_cluster(mapa_rank(smem_u32(acc_empty + b), 0));
-          if (gc == nchunks_group - 1) mbar_arrive_cluster(mapa_rank(smem_u32(group_done), 0));
+          __syncwarp();
+          if (lane == 0) {
+            mbar_arrive_cluster(mapa_rank(smem_u32(acc_empty + b), 0));
+            if (gc == nchunks_group - 1) mbar_arrive_cluster(mapa_rank(smem_u32(group_done), 0));
+          }
         }
       }
       if (stored && !ok) {
@@ -771,6 +780,7 @@ static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 // is how the expiry path is tested.
 #include <atomic>
 static std::atomic<unsigned long long> g_wait_ns{WAIT_NS};
+constexpr int PREP_BATCH = 4;
 extern "C" void pg_set_wait_limit_ns(unsigned long long ns) { g_wait_ns.store(ns ? ns : WAIT_NS); }
 extern "C" unsigned long long pg_wait_limit_ns(void) { return g_wait_ns.load(); }
 
@@ -816,6 +826,21 @@ static int gemm_cta_capacity() {
   return g_cap[dev];
 }
 
+// Frequencies per B-digit preparation pass (process-wide, read by every
+// layout computation after it is set, workspace queries included).  A pass
+// reads the five A digit planes once and writes the five B planes of each of
+// its frequencies, so a longer pass cuts the A reads per frequency (at C3 a
+// frequency's B planes are 24.4 GB and the A planes 24.4 GB: 36.6 GB of
+// traffic per frequency with two per pass, 30.5 GB with four) at the cost of
+// one set of B planes of workspace per frequency.  0 restores the default, 4.
+static std::atomic<int> g_prep_batch{PREP_BATCH};
+extern "C" int pg_set_chi0_prep_batch(int n) {
+  if (n < 0 || n > 64) return PG_EARG;
+  g_prep_batch.store(n ? n : PREP_BATCH);
+  return PG_OK;
+}
+extern "C" int pg_chi0_prep_batch(void) { return g_prep_batch.load(); }
+
 static MixedLayout mixed_layout(int nb1, int nb2, int nkp, int npb, int wb, int kb_split, long long K = -1) {
   MixedLayout L;
   L.K = K >= 0 ? K : (long long)nkp * nb1 * nb2;
@@ -852,10 +877,11 @@ static MixedLayout mixed_layout(int nb1, int nb2, int nkp, int npb, int wb, int 
   L.kb_per_split = (L.nkb + L.nsplit - 1) / L.nsplit;
   L.nsplit = (L.nkb + L.kb_per_split - 1) / L.kb_per_split;   // no empty split
   L.wb = wb;
-  // B digits are prepared for at least two frequencies per pass over the A
-  // digits (each pass reads all five A planes), while the GEMM may take one
-  // frequency per launch
-  L.wbp = wb < 2 ? 2 : wb;
+  // B digits are prepared for several frequencies per pass over the A digits
+  // (each pass reads all five A planes; see pg_set_chi0_prep_batch), a whole
+  // number of GEMM batches, while the GEMM may take one frequency per launch
+  const int pb = g_prep_batch.load();
+  L.wbp = wb >= pb ? wb : (pb + wb - 1) / wb * wb;
   size_t o = 0;
   L.off_adig = o; o += al256((size_t)S * L.R_pad * L.K_pad * 2);
   L.off_bdig = o; o += al256((size_t)L.wbp * S * L.R_pad * L.K_pad * 2);
@@ -933,8 +959,15 @@ static int chi0_mixed_impl(const void* minm, int nkp, int k0, const int* kstart,
   double* out = (double*)(w + L.off_out);
   const double2* M = (const double2*)minm;
 
-  // padding rows of the digit arrays must be zero
-  if (cudaMemsetAsync(adig, 0, (size_t)S * L.R_pad * L.K_pad * 2, s) != cudaSuccess) return PG_ECUDA;
+  // padding rows of the digit arrays must be zero: no pass writes them, so
+  // they are cleared once per contraction (rows R … R_pad−1 of every
+  // (plane, K-block) slice, R_pad·128 bytes apart)
+  if (L.R_pad > L.R) {
+    const size_t pitch = (size_t)L.R_pad * KB * 2, off = (size_t)L.R * KB * 2, width = pitch - off;
+    if (cudaMemset2DAsync((char*)adig + off, pitch, 0, width, (size_t)S * L.nkb, s) != cudaSuccess ||
+        cudaMemset2DAsync((char*)bdig + off, pitch, 0, width, (size_t)L.wbp * S * L.nkb, s) != cudaSuccess)
+      return PG_ECUDA;
+  }
   if (cudaMemsetAsync(tmax, 0, (size_t)L.R_pad * L.nkb * 4, s) != cudaSuccess) return PG_ECUDA;
   k_block_max<<<dim3((npb + 127) / 128, L.nkb), 128, 0, s>>>(M, L.K, npb, L.R_pad, L.nkb, tmax);
   k_row_exp_A<<<L.R_pad, 256, 0, s>>>(tmax, L.R, L.R_pad, L.nkb, eA);
@@ -967,8 +1000,8 @@ static int chi0_mixed_impl(const void* minm, int nkp, int k0, const int* kstart,
     k_weights_prep<<<dim3(L.nkb, npw0), 64, 0, s>>>(kcw, nb1, nb2, nkp_total, k0, nkp, kstart, knb2, 0, npw0, coef,
                                                     L.K, L.K_pad, wpair);
     if (cudaMemsetAsync(rmax, 0, rstride * 4, s) != cudaSuccess) return PG_ECUDA;
-    k_rowmax_B<<<dim3((unsigned)((L.K_pad + 1023) / 1024), L.R_pad), 256, 0, s>>>(adig, wpair, L.R, L.R_pad, L.K_pad,
-                                                                                  npw0, rmax);
+    k_rowmax_B<<<dim3((unsigned)((L.K_pad + 1023) / 1024), L.R), 256, 0, s>>>(adig, wpair, L.R, L.R_pad, L.K_pad,
+                                                                              npw0, rmax);
     pg_count_launches(2);
   }
   for (int op0 = 0, bi = 0; op0 < nom; op0 += wbp, bi++) {
@@ -988,7 +1021,8 @@ static int chi0_mixed_impl(const void* minm, int nkp, int k0, const int* kstart,
       if (cudaMemsetAsync(rnxt, 0, rstride * 4, s) != cudaSuccess) return PG_ECUDA;
       pg_count_launches(1);
     }
-    k_digits_B<<<dim3((unsigned)((L.nkb + DB_KB - 1) / DB_KB), L.R_pad / DB_ROWS), 256,
+    // real rows only (rounded up to whole row blocks; the rest stay zero)
+    k_digits_B<<<dim3((unsigned)((L.nkb + DB_KB - 1) / DB_KB), (L.R + DB_ROWS - 1) / DB_ROWS), 256,
                  (size_t)(npn > 0 ? npn : 1) * DB_ROWS * sizeof(float), s>>>(
         adig, eA, wcur, fB, L.R, L.R_pad, L.K_pad, npw, bdig, npn > 0 ? wnxt : nullptr, npn, rnxt);
     pg_count_launches(2);

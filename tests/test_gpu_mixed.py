@@ -64,12 +64,16 @@ def test_digit_gemm_is_exact_white_box():
         n = int(np.prod(shape)) * np.dtype(dtype).itemsize
         return raw[offs[i]:offs[i] + n].view(dtype).reshape(shape)
 
+    # the workspace holds the last preparation pass (wbp frequencies from op0)
+    # and the last GEMM launch (frequencies from om0, B slot om0 − op0)
+    wbp = -(-max(wb, lib.pg_chi0_prep_batch()) // wb) * wb
+    om0 = (nom - 1) // wb * wb
+    slot = om0 - om0 // wbp * wbp
     # digit arrays are K-block major: [plane][K-block][row][64]
     A = _bf16(view(0, np.uint16, (S, nkb, R_pad, 64)).transpose(0, 2, 1, 3).reshape(S, R_pad, K_pad))
-    B = _bf16(view(1, np.uint16, (wb, S, nkb, R_pad, 64)).transpose(0, 1, 3, 2, 4).reshape(wb, S, R_pad, K_pad))[0]
-    # (last batch: frequency nom-1 in slot 0)
+    B = _bf16(view(1, np.uint16, (wbp, S, nkb, R_pad, 64)).transpose(0, 1, 3, 2, 4).reshape(wbp, S, R_pad, K_pad))[slot]
     eA = view(5, np.int32, (R_pad,))
-    fB = view(6, np.int32, (wb, R_pad))[0]
+    fB = view(6, np.int32, (wbp, R_pad))[slot]
     out = view(7, np.float64, (nsplit, wb, npair, 128, 128))[:, 0]
     assert np.abs(A).max() <= 129 and np.abs(B).max() <= 129
 
@@ -81,7 +85,7 @@ def test_digit_gemm_is_exact_white_box():
     scal = 2.0 ** -(8.0 * (np.arange(S) + 1))
     Vrec = np.einsum("srk,s->rk", A, scal) * 2.0 ** eA[:, None]
     assert np.all(np.abs(Vrec - V) <= 2.0 ** (eA[:, None] - 40.0))
-    cw = -2.0 * np.array([kcw[:, :, ik, nom - 1].ravel() for ik in range(nkp)]).ravel()
+    cw = -2.0 * np.array([kcw[:, :, ik, om0].ravel() for ik in range(nkp)]).ravel()
     cw = np.concatenate([cw, np.zeros(K_pad - K)])
     Brec = np.einsum("srk,s->rk", B, scal) * 2.0 ** fB[:, None]
     assert np.all(np.abs(Brec - Vrec * cw[None, :]) <= 2.0 ** (fB[:, None] - 38.0))

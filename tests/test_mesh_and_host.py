@@ -148,9 +148,39 @@ def test_mixed_layout_keeps_group_sums_exact(nb1, nb2, nkp, npb, wb, kb_split):
     o = list(offs)
     assert all(x % 256 == 0 for x in o[:8]) and o == sorted(o)
     assert o[1] - o[0] >= 5 * R_pad * K_pad * 2                      # A digit planes
-    assert o[2] - o[1] >= max(2, wb) * 5 * R_pad * K_pad * 2         # B digit planes
+    wbp = -(-max(wb, lib.pg_chi0_prep_batch()) // wb) * wb          # frequencies per B-digit pass
+    assert o[2] - o[1] >= wbp * 5 * R_pad * K_pad * 2                # B digit planes
     assert o[8] - o[7] >= nsplit * wb * npair * 128 * 128 * 8        # group-sum tiles
     assert lib.pg_chi0_mixed_workspace(nb1, nb2, nkp, npb, wb, kb_split) == o[8]
+
+
+def test_chi0_prep_batch_setting():
+    """Frequencies per B-digit pass: default 4, settable in [1, 64] (0 restores
+    the default), whole GEMM batches, one set of five B planes per frequency
+    in the workspace."""
+    from pygw_gb300 import _lib
+    lib = _lib.load()
+    assert lib.pg_chi0_prep_batch() == 4
+    args = (23, 192, 8, 300, 1, 0)
+    base = lib.pg_chi0_mixed_workspace(*args)
+    offs = (ctypes.c_size_t * 9)()
+    dims = (ctypes.c_longlong * 9)()
+    assert lib.pg_chi0_mixed_layout(*args, offs, dims) == 0
+    plane = 5 * dims[3] * dims[1] * 2                                   # five planes of R_pad × K_pad bf16
+    try:
+        for bad in (-1, 65):
+            assert lib.pg_set_chi0_prep_batch(bad) == -1
+            assert lib.pg_chi0_prep_batch() == 4
+        assert lib.pg_set_chi0_prep_batch(2) == 0 and lib.pg_chi0_prep_batch() == 2
+        two = lib.pg_chi0_mixed_workspace(*args)
+        assert base - two >= 2 * plane and base - two < 2 * plane + 4096 + 2 * 4 * dims[1] * 8
+        # omega_batch 3 with a pass of 4: two whole launches, six frequencies
+        assert lib.pg_set_chi0_prep_batch(4) == 0
+        assert lib.pg_chi0_mixed_layout(23, 192, 8, 300, 3, 0, offs, dims) == 0
+        assert offs[2] - offs[1] >= 6 * plane
+    finally:
+        lib.pg_set_chi0_prep_batch(0)
+    assert lib.pg_chi0_prep_batch() == 4 and lib.pg_chi0_mixed_workspace(*args) == base
 
 
 def test_polarization_entry_points_validate_on_the_host():
