@@ -44,17 +44,23 @@ namespace pgw {
 #define TOL_UNPHYS 1.0e4
 #define TOL_TAYLOR 10.0
 
+struct SubTet;
+
 struct Params {
   const double* enk;   // [nbnd][nkp] column-major: enk[b + nbnd*k]
   const int* kqid;     // [nkp]
   const double* omega; // [nom]
   const int* tetc;     // [ntet][4]: tetc[i + 4*t]
   double* scratch;     // [ntet][4][nomc][P]
-  const int* order;    // items sorted by polyhedron class (null: natural order)
+  const int* order;    // items of the chunk sorted by polyhedron class
+  SubTet* recs;        // set-up sub-tetrahedra of the chunk's items (≤ 6 per item)
+  int* recoff;         // [chunk items] first record of each contributing item
+  unsigned* nrec;      // records claimed so far in the chunk
   unsigned* status;    // device status word (may be null)
   unsigned long long* counters;  // PG_NCOUNTERS (may be null)
   double ef;
   int nbnd, nkp, ncg, numin, nb1, nb2, ntet, om0, nomc;
+  int tet0;            // first tetrahedron of the chunk
 };
 
 struct Ctx {
@@ -386,6 +392,10 @@ __device__ __forceinline__ void check_weight(double& w, double omeg, Ctx& cx) {
   }
 }
 
+__device__ __forceinline__ double pick5(const double (&a)[5], int i) {
+  return i == 0 ? a[0] : i == 1 ? a[1] : i == 2 ? a[2] : i == 3 ? a[3] : a[4];
+}
+
 // Weights of one sub-tetrahedron at one frequency, already mapped to the
 // big-tetrahedron corners and multiplied by the sub-tetrahedron volume
 // (generictetra_par's epilogue, for_tetrahedra3.f90:392-403).
@@ -394,11 +404,21 @@ __device__ void eval_subtet(const SubTet& s, double omeg, double wout[4], Ctx& c
   if (omeg > s.taylor_omega) {
     stweight_itaylor(s.ds, omeg, ws);
   } else {
-    double T[5], L[5];
-    for (int q = 0; q < s.nval; q++) {
+    // T, L of the distinct corner values, kept in registers (the vertex
+    // formulas pick them by the record's node map through pick5); one copy
+    // of the atan/log code in a loop, its results moved into place by selects
+    double T[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, L[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    const int nval = s.nval;
+#pragma unroll 1
+    for (int q = 0; q < nval; q++) {
       const double x = s.val[q];
-      T[q] = (omeg > OMEG_TINY) ? pg_atan(x / omeg) : copysign(1.0, x) * 2.0 * pg_atan(1.0);
-      L[q] = ((omeg * omeg + x * x) > 1.0e-10) ? pg_log(x * x + omeg * omeg) : 0.0;
+      const double t = (omeg > OMEG_TINY) ? pg_atan(x / omeg) : copysign(1.0, x) * 2.0 * pg_atan(1.0);
+      const double l = ((omeg * omeg + x * x) > 1.0e-10) ? pg_log(x * x + omeg * omeg) : 0.0;
+#pragma unroll
+      for (int i = 0; i < 5; i++) {
+        T[i] = (q == i) ? t : T[i];
+        L[i] = (q == i) ? l : L[i];
+      }
     }
     const double omeg2 = omeg * omeg;
     double wt[4];
@@ -410,8 +430,8 @@ __device__ void eval_subtet(const SubTet& s, double omeg, double wout[4], Ctx& c
           const double* evt = c;
           const double* evw = c + 9;
           const int* m = s.map[v];
-          const double t1 = T[m[0]], t2 = T[m[1]], t3 = T[m[2]], t4 = T[m[3]];
-          const double l1 = L[m[0]], l2 = L[m[1]], l3 = L[m[2]], l4 = L[m[3]];
+          const double t1 = pick5(T, m[0]), t2 = pick5(T, m[1]), t3 = pick5(T, m[2]), t4 = pick5(T, m[3]);
+          const double l1 = pick5(L, m[0]), l2 = pick5(L, m[1]), l3 = pick5(L, m[2]), l4 = pick5(L, m[3]);
           double aa = evt[1] + omeg2 * evw[1] + omeg * (t1 * evt[2] + t2 * evt[3] + t3 * evt[4] + t4 * evt[5] +
                                                         omeg2 * (t1 * evw[2] + t2 * evw[3] + t3 * evw[4] + t4 * evw[5]));
           double bb = l1 * evt[6] + l2 * evt[7] + l3 * evt[8] + l4 * evt[9] +
@@ -427,8 +447,8 @@ __device__ void eval_subtet(const SubTet& s, double omeg, double wout[4], Ctx& c
           const double* evt = c;
           const double* evw = c + 7;
           const int* m = s.map[v];
-          const double t1 = T[m[0]], t3 = T[m[2]], t4 = T[m[3]];
-          const double l1 = L[m[0]], l3 = L[m[2]], l4 = L[m[3]];
+          const double t1 = pick5(T, m[0]), t3 = pick5(T, m[2]), t4 = pick5(T, m[3]);
+          const double l1 = pick5(L, m[0]), l3 = pick5(L, m[2]), l4 = pick5(L, m[3]);
           double aa = evt[1] + omeg2 * evw[1] + omeg * (t1 * evt[2] + t3 * evt[3] + t4 * evt[4] +
                                                         omeg2 * (t1 * evw[2] + t3 * evw[3] + t4 * evw[4]));
           double bb = l1 * evt[5] + l3 * evt[6] + l4 * evt[7] + omeg2 * (l1 * evw[5] + l3 * evw[6] + l4 * evw[7]);
@@ -474,8 +494,16 @@ __device__ void eval_subtet(const SubTet& s, double omeg, double wout[4], Ctx& c
         cx.status |= PG_ERR_EQUIV;
         break;
     }
+    // ws[ind[i] − 1] = wt[i] in i order, as register selects (the last
+    // write to a slot wins, slots never written keep 0)
+    int ind[4];
 #pragma unroll
-    for (int i = 0; i < 4; i++) ws[s.ind[i] - 1] = wt[i];
+    for (int i = 0; i < 4; i++) ind[i] = s.ind[i] - 1;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+        if (ind[i] == j) ws[j] = wt[i];
   }
   double sm = ws[0];
   sm = sm + ws[1];
@@ -862,51 +890,6 @@ __device__ int sortnodes(const Nodes& N, int index[9][2], Ctx& cx) {
   return info;
 }
 
-// ------------------------------------------------------------ phase 1 kernel
-// Writes (mode 0) or adds (mode 1) one sub-tetrahedron's weights for all
-// frequencies of the chunk into the thread's scratch slots.
-__device__ void subtet_all_omega(SubTet& s, const double e[4], const double f[4], const Params& p, double* out,
-                                 size_t cstride, size_t wstride, int mode, Ctx& cx) {
-  setup_subtet(s, e, f, cx);
-  if (s.vol < ZTOL_VOL) {
-    cx.cnt[PG_CNT_ZERO_VOL]++;
-    if (mode == 0)
-      for (int w = 0; w < p.nomc; w++)
-        for (int c = 0; c < 4; c++) out[c * cstride + w * wstride] = 0.0;
-    return;
-  }
-  cx.cnt[PG_CNT_EQ4 + (s.flag == 4 ? 0 : s.flag == 6 ? 1 : s.flag == 8 ? 2 : s.flag == 10 ? 3 : 4)]++;
-  for (int w = 0; w < p.nomc; w++) {
-    const double omeg = p.omega[p.om0 + w];
-    double wo[4];
-    eval_subtet(s, omeg, wo, cx);
-    if (omeg > s.taylor_omega) cx.cnt[PG_CNT_TAYLOR]++; else cx.cnt[PG_CNT_EXACT]++;
-#pragma unroll
-    for (int c = 0; c < 4; c++) {
-      double* d = out + c * cstride + w * wstride;
-      *d = (mode == 0) ? wo[c] : (*d + wo[c]);
-    }
-  }
-}
-
-// One sub-tetrahedron at a single frequency (setup recomputed): used for the
-// second half of 7- and 8-node polyhedra, whose two halves the reference sums
-// separately before adding them.
-__device__ void subtet_one_omega(SubTet& s, const double e[4], const double f[4], double omeg, double acc[4],
-                                 bool first, bool count_setup, Ctx& cx) {
-  setup_subtet(s, e, f, cx);
-  double wo[4] = {0.0, 0.0, 0.0, 0.0};
-  if (s.vol >= ZTOL_VOL) {
-    if (count_setup) cx.cnt[PG_CNT_EQ4 + (s.flag == 4 ? 0 : s.flag == 6 ? 1 : s.flag == 8 ? 2 : s.flag == 10 ? 3 : 4)]++;
-    eval_subtet(s, omeg, wo, cx);
-    if (omeg > s.taylor_omega) cx.cnt[PG_CNT_TAYLOR]++; else cx.cnt[PG_CNT_EXACT]++;
-  } else if (count_setup) {
-    cx.cnt[PG_CNT_ZERO_VOL]++;
-  }
-#pragma unroll
-  for (int c = 0; c < 4; c++) acc[c] = first ? (0.0 + wo[c]) : (acc[c] + wo[c]);
-}
-
 // Corner energies of item (tetrahedron, band pair) and its integration
 // polyhedron: surfnodes → unrepnodes → relnodes → sortnodes
 // (for_tetrahedra3.f90:3-136 up to the nnod dispatch).  Returns true when
@@ -973,37 +956,73 @@ __device__ void place_nodes(const Nodes& N, const int index[9][2], double tc[2][
 // volume tolerance, 1..5: sorteq case 4/6/8/10/16).  Items of one class run
 // the same code path, so sorting by class keeps warps converged.
 constexpr int NCLASS = 32;
-__device__ int item_class(const Params& p, long long item) {
-  Ctx cx;
-  cx.status = 0;
-  for (int i = 0; i < PG_NCOUNTERS; i++) cx.cnt[i] = 0;
-  Item it;
-  Nodes N;
-  int index[9][2];
-  if (item_geometry(p, item, it, N, index, cx) || cx.status) return 0;
-  SubTet s;
-  if (N.nnod == 4) {
-    for (int n = 0; n < 4; n++) for (int c = 0; c < 3; c++) s.corner[n][c] = N.x[n + 1][c];
-  } else {
-    double tc[2][6][3];
-    place_nodes(N, index, tc, cx);
-    for (int n = 0; n < 4; n++) for (int c = 0; c < 3; c++) s.corner[n][c] = tc[0][n][c];
-  }
-  setup_subtet(s, it.e, it.f, cx);
-  const int g = (s.vol < ZTOL_VOL) ? 0 : s.flag == 4 ? 1 : s.flag == 6 ? 2 : s.flag == 8 ? 3 : s.flag == 10 ? 4 : 5;
-  return 1 + 6 * (N.nnod - 4) + g;
-}
+__host__ __device__ constexpr int class_nnod(int c) { return (c - 1) / 6 + 4; }
+// Sub-tetrahedra per polyhedron half: 1 (4 nodes), 2 (pentahedron: 5 or 7
+// nodes), 3 (prism: 6 or 8); 7 and 8 nodes have two halves.
+__host__ __device__ constexpr int nodes_nsub(int nnod) { return nnod == 4 ? 1 : (nnod == 5 || nnod == 7) ? 2 : 3; }
+__host__ __device__ constexpr int nodes_ngroup(int nnod) { return nnod >= 7 ? 2 : 1; }
+constexpr int MAX_SUBTET = 6;   // sub-tetrahedra of one item at most (8 nodes: 2 × 3)
 
-__global__ void __launch_bounds__(128) k_tet_classify(Params p, long long nitems, unsigned char* cls,
+// Geometry pass over the items of one tetrahedron chunk (frequency-
+// independent): builds the integration polyhedron of each item
+// (item_geometry), splits it into sub-tetrahedra (place_nodes, the
+// genericfunf_par / genericprism_par corner order), sets each one up
+// (setup_subtet: volume, sorteq grouping, closed-form coefficients) and
+// stores the set-up sub-tetrahedra as records for k_tet_eval, the item's
+// first record index in recoff and its class in cls.  Records are
+// claimed with one atomic per item; their order in the array does not matter
+// (each item reads back only its own, in its own order).  The per-item and
+// per-sub-tetrahedron counters (calls, node counts, groupings, zero volumes)
+// are counted here, once.
+__global__ void __launch_bounds__(128) k_tet_geometry(Params p, long long nitems, unsigned char* cls,
                                                       unsigned* hist) {
   __shared__ unsigned h[NCLASS];
   if (threadIdx.x < NCLASS) h[threadIdx.x] = 0;
   __syncthreads();
-  const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (item < nitems) {
-    const int c = item_class(p, item);
-    cls[item] = (unsigned char)c;
-    atomicAdd(&h[c], 1u);
+  const long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (li < nitems) {
+    Ctx cx;
+    cx.status = 0;
+    for (int i = 0; i < PG_NCOUNTERS; i++) cx.cnt[i] = 0;
+    const int P = p.nb1 * p.nb2;
+    const long long item = (long long)p.tet0 * P + li;
+    Item it;
+    Nodes N;
+    int index[9][2];
+    int cl = 0;
+    if (!item_geometry(p, item, it, N, index, cx)) {
+      const int nnod = N.nnod;
+      const int nsub = nodes_nsub(nnod), ngroup = nodes_ngroup(nnod);
+      const unsigned r0 = atomicAdd(p.nrec, (unsigned)(nsub * ngroup));
+      p.recoff[li] = (int)r0;
+      double tc[2][6][3];
+      if (nnod > 4) place_nodes(N, index, tc, cx);
+      int g0 = 0;
+      for (int g = 0; g < ngroup; g++) {
+        for (int st = 0; st < nsub; st++) {
+          SubTet& s = p.recs[r0 + g * nsub + st];
+          for (int n = 0; n < 4; n++)
+            for (int c = 0; c < 3; c++) s.corner[n][c] = (nnod == 4) ? N.x[n + 1][c] : tc[g][st + n][c];
+          setup_subtet(s, it.e, it.f, cx);
+          int grp = 0;
+          if (s.vol < ZTOL_VOL) {
+            cx.cnt[PG_CNT_ZERO_VOL]++;
+          } else {
+            grp = s.flag == 4 ? 1 : s.flag == 6 ? 2 : s.flag == 8 ? 3 : s.flag == 10 ? 4 : 5;
+            cx.cnt[PG_CNT_EQ4 + grp - 1]++;
+          }
+          if (g == 0 && st == 0) g0 = grp;
+        }
+      }
+      cl = 1 + 6 * (nnod - 4) + g0;
+    }
+    cls[li] = (unsigned char)cl;
+    atomicAdd(&h[cl], 1u);
+    if (p.status && cx.status) atomicOr(p.status, cx.status);
+    if (p.counters) {
+      for (int i = 0; i < PG_NCOUNTERS; i++)
+        if (cx.cnt[i]) atomicAdd(p.counters + i, cx.cnt[i]);
+    }
   }
   __syncthreads();
   if (threadIdx.x < NCLASS && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
@@ -1038,72 +1057,90 @@ __global__ void k_class_scatter(const unsigned char* cls, long long nitems, unsi
   if (in) order[base + rank] = (int)item;
 }
 
-__global__ void __launch_bounds__(128) k_tet_weights(Params p) {
-  const int P = p.nb1 * p.nb2;
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)P * p.ntet) return;
-  const long long item = p.order ? (long long)p.order[idx] : idx;
+// Evaluation pass: one thread per (item of the chunk in class order,
+// frequency), the frequency fastest, so a warp covers one or two items and
+// follows one code path.  Each thread evaluates its item's sub-tetrahedra at
+// its frequency from the records (read through L1; the lanes of an item read
+// the same addresses) and writes the four corner weights into the scratch
+// slots, summing exactly as the reference does: the first polyhedron's
+// sub-tetrahedra in order (generictetra_par results added one by one), the
+// second polyhedron of a 7- or 8-node item summed separately from 0 and then
+// added (for_tetrahedra3.f90:60-131).
+__global__ void __launch_bounds__(128) k_tet_eval(Params p, long long nitems, const unsigned char* __restrict__ cls) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool in = t < nitems * p.nomc;
   Ctx cx;
   cx.status = 0;
-  for (int i = 0; i < PG_NCOUNTERS; i++) cx.cnt[i] = 0;
-  Item it;
-  Nodes N;
-  int index[9][2];
-  bool zero = item_geometry(p, item, it, N, index, cx);
-  const double* e = it.e;
-  const double* f = it.f;
-  const size_t wstride = (size_t)P;
-  const size_t cstride = (size_t)p.nomc * P;
-  double* out = p.scratch + (size_t)it.tet * 4 * cstride + it.pair;
-  if (zero) {
-    for (int w = 0; w < p.nomc; w++)
-      for (int c = 0; c < 4; c++) out[c * cstride + w * wstride] = 0.0;
-  } else {
-    SubTet s;
-    const int nnod = N.nnod;
-    if (nnod == 4) {
-      for (int n = 0; n < 4; n++)
-        for (int c = 0; c < 3; c++) s.corner[n][c] = N.x[n + 1][c];
-      subtet_all_omega(s, e, f, p, out, cstride, wstride, 0, cx);
-    } else {
-      const int cap = (nnod == 5 || nnod == 7) ? 5 : 6;
-      const int nsub = cap - 3;                     // 2 tets per pentahedron, 3 per prism
-      const int ngroup = (nnod >= 7) ? 2 : 1;
-      double tc[2][6][3];
-      place_nodes(N, index, tc, cx);
-      // First (or only) polyhedron: sub-tetrahedra (a, a+1, a+2, a+3), summed
-      // in order straight into the scratch slots.
-      for (int st = 0; st < nsub; st++) {
-        for (int n = 0; n < 4; n++) for (int c = 0; c < 3; c++) s.corner[n][c] = tc[0][st + n][c];
-        subtet_all_omega(s, e, f, p, out, cstride, wstride, st == 0 ? 0 : 1, cx);
-      }
-      if (ngroup == 2) {
-        for (int w = 0; w < p.nomc; w++) {
-          const double omeg = p.omega[p.om0 + w];
-          double acc[4];
-          for (int st = 0; st < nsub; st++) {
-            for (int n = 0; n < 4; n++) for (int c = 0; c < 3; c++) s.corner[n][c] = tc[1][st + n][c];
-            subtet_one_omega(s, e, f, omeg, acc, st == 0, w == 0, cx);
-          }
+  cx.cnt[PG_CNT_BIGW_WARN] = 0;
+  cx.cnt[PG_CNT_BIGW_ZEROED] = 0;
+  unsigned n_exact = 0, n_taylor = 0;
+  if (in) {
+    const int P = p.nb1 * p.nb2;
+    const long long pos = t / p.nomc;
+    const int w = (int)(t - pos * p.nomc);
+    const int li = p.order[pos];
+    const long long item = (long long)p.tet0 * P + li;
+    const int tet = (int)(item / P), pair = (int)(item - (long long)tet * P);
+    const size_t cstride = (size_t)p.nomc * P;
+    double* out = p.scratch + (size_t)tet * 4 * cstride + (size_t)w * P + pair;
+    const int cl = cls[li];
+    double o[4] = {0.0, 0.0, 0.0, 0.0};
+    if (cl != 0) {
+      const double omeg = p.omega[p.om0 + w];
+      const int nnod = class_nnod(cl);
+      const int nsub = nodes_nsub(nnod);
+      const SubTet* r = p.recs + p.recoff[li];
+      // records in order: the first polyhedron's nsub sub-tetrahedra, then
+      // (7, 8 nodes) the second's; one evaluation site keeps the code small
+      const int nrec = nsub * nodes_ngroup(nnod);
+      double acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll 1
+      for (int i = 0; i < nrec; i++) {
+        const SubTet& s = r[i];
+        const bool second = i >= nsub;
+        const int st = second ? i - nsub : i;
+        double wo[4] = {0.0, 0.0, 0.0, 0.0};
+        const bool live = s.vol >= ZTOL_VOL;
+        if (live) {
+          eval_subtet(s, omeg, wo, cx);
+          if (omeg > s.taylor_omega) n_taylor++; else n_exact++;
+        }
+        if (!second) {
+          // the first one sets the slots (0.0 below the volume tolerance),
+          // later ones below the tolerance add nothing
 #pragma unroll
-          for (int c = 0; c < 4; c++) {
-            double* d = out + c * cstride + w * wstride;
-            *d = *d + acc[c];
+          for (int c = 0; c < 4; c++) o[c] = (st == 0) ? wo[c] : (live ? o[c] + wo[c] : o[c]);
+        } else {
+          // the second polyhedron sums from 0 on its own, then adds in
+#pragma unroll
+          for (int c = 0; c < 4; c++) acc[c] = (st == 0) ? (0.0 + wo[c]) : (acc[c] + wo[c]);
+          if (st == nsub - 1) {
+#pragma unroll
+            for (int c = 0; c < 4; c++) o[c] = o[c] + acc[c];
           }
         }
       }
-    }
-  }
-  // Non-finite check and status/counter flush.
-  if (!zero) {
-    for (int w = 0; w < p.nomc; w++)
+#pragma unroll
       for (int c = 0; c < 4; c++)
-        if (!isfinite(out[c * cstride + w * wstride])) cx.status |= PG_ERR_NONFINITE;
+        if (!isfinite(o[c])) cx.status |= PG_ERR_NONFINITE;
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) out[c * cstride] = o[c];
   }
-  if (p.status && cx.status) atomicOr(p.status, cx.status);
-  if (p.counters) {
-    for (int i = 0; i < PG_NCOUNTERS; i++)
-      if (cx.cnt[i]) atomicAdd(p.counters + i, cx.cnt[i]);
+  // status and counters: one atomic per warp
+  const unsigned st_w = __reduce_or_sync(0xffffffffu, cx.status);
+  const unsigned ex_w = __reduce_add_sync(0xffffffffu, n_exact);
+  const unsigned ty_w = __reduce_add_sync(0xffffffffu, n_taylor);
+  const unsigned bw_w = __reduce_add_sync(0xffffffffu, (unsigned)cx.cnt[PG_CNT_BIGW_WARN]);
+  const unsigned bz_w = __reduce_add_sync(0xffffffffu, (unsigned)cx.cnt[PG_CNT_BIGW_ZEROED]);
+  if ((threadIdx.x & 31) == 0) {
+    if (p.status && st_w) atomicOr(p.status, st_w);
+    if (p.counters) {
+      if (ex_w) atomicAdd(p.counters + PG_CNT_EXACT, (unsigned long long)ex_w);
+      if (ty_w) atomicAdd(p.counters + PG_CNT_TAYLOR, (unsigned long long)ty_w);
+      if (bw_w) atomicAdd(p.counters + PG_CNT_BIGW_WARN, (unsigned long long)bw_w);
+      if (bz_w) atomicAdd(p.counters + PG_CNT_BIGW_ZEROED, (unsigned long long)bz_w);
+    }
   }
 }
 
@@ -1183,12 +1220,88 @@ using namespace pgw;
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// Frequency-independent part of the workspace: k → slot lists (CSR) and the
-// per-item class and sorted order.
-static size_t lists_bytes(int nkp, int ntet, long long items) {
-  return align256(sizeof(int) * (size_t)(nkp + 1)) + align256(sizeof(int) * (size_t)nkp) +
-         align256(sizeof(int) * (size_t)4 * ntet) + align256((size_t)items) + align256(sizeof(int) * (size_t)items) +
-         2 * align256(sizeof(unsigned) * NCLASS);
+// Workspace of the weight passes: the k → slot lists (CSR), the per-chunk
+// item arrays (class, class order, first record), the class histogram and
+// record counter, the sub-tetrahedron records of one tetrahedron chunk, and
+// the scratch weights [ntet][4][nomc][P] (plus the SVD-projected copy for
+// par3).  The chunk is the most tetrahedra whose records fit in rec_budget
+// even when every item yields the maximum of six sub-tetrahedra.
+constexpr size_t REC_BUDGET = 1ull << 30;
+struct WLayout {
+  int tpc;   // tetrahedra per chunk
+  size_t kptr, kcount, kslot, cls, order, recoff, hist, cursor, recs, scratch, scratch2, total;
+};
+static WLayout weights_layout(int nkp, int ntet, long long P, int nomc, int nl, size_t rec_budget) {
+  WLayout L;
+  long long tpc = (long long)(rec_budget / ((size_t)P * MAX_SUBTET * sizeof(SubTet)));
+  if (tpc < 1) tpc = 1;
+  if (tpc > ntet) tpc = ntet;
+  L.tpc = (int)tpc;
+  const size_t ci = (size_t)tpc * P;
+  size_t o = 0;
+  L.kptr = o; o += align256(sizeof(int) * (size_t)(nkp + 1));
+  L.kcount = o; o += align256(sizeof(int) * (size_t)nkp);
+  L.kslot = o; o += align256(sizeof(int) * (size_t)4 * ntet);
+  L.cls = o; o += align256(ci);
+  L.order = o; o += align256(sizeof(int) * ci);
+  L.recoff = o; o += align256(sizeof(int) * ci);
+  L.hist = o; o += align256(sizeof(unsigned) * (NCLASS + 1));
+  L.cursor = o; o += align256(sizeof(unsigned) * NCLASS);
+  L.recs = o; o += align256(ci * MAX_SUBTET * sizeof(SubTet));
+  L.scratch = o; o += align256(sizeof(double) * (size_t)4 * ntet * nomc * P);
+  L.scratch2 = o; o += nl > 0 ? align256(sizeof(double) * (size_t)4 * ntet * nl * P) : 0;
+  L.total = o;
+  return L;
+}
+
+// k → (tetrahedron, corner) slot lists.
+static void enqueue_kcsr(const WLayout& L, char* w, const int* tetc, int ntet, int nkp, cudaStream_t s) {
+  int* kptr = (int*)(w + L.kptr);
+  int* kcount = (int*)(w + L.kcount);
+  int* kslot = (int*)(w + L.kslot);
+  k_kcsr_count<<<(nkp + 127) / 128, 128, 0, s>>>(tetc, ntet, nkp, kcount);
+  k_kcsr_scan<<<1, 1, 0, s>>>(kcount, nkp, kptr);
+  k_kcsr_fill<<<(nkp + 127) / 128, 128, 0, s>>>(tetc, ntet, nkp, kptr, kslot);
+  pg_count_launches(3);
+}
+
+// Scratch weights of frequencies om0 … om0+nomc−1 (p.om0, p.nomc) for every
+// tetrahedron, chunk by chunk: geometry and records, class order, evaluation.
+static int enqueue_tet_weights(Params p, const WLayout& L, char* w, cudaStream_t s) {
+  unsigned char* cls = (unsigned char*)(w + L.cls);
+  unsigned* hist = (unsigned*)(w + L.hist);
+  unsigned* cursor = (unsigned*)(w + L.cursor);
+  int* order = (int*)(w + L.order);
+  p.order = order;
+  p.recoff = (int*)(w + L.recoff);
+  p.recs = (SubTet*)(w + L.recs);
+  p.nrec = hist + NCLASS;
+  const long long P = (long long)p.nb1 * p.nb2;
+  for (int t0 = 0; t0 < p.ntet; t0 += L.tpc) {
+    const int ntc = (t0 + L.tpc <= p.ntet) ? L.tpc : p.ntet - t0;
+    const long long ni = (long long)ntc * P;
+    const unsigned nblk = (unsigned)((ni + 127) / 128);
+    p.tet0 = t0;
+    if (cudaMemsetAsync(hist, 0, sizeof(unsigned) * (NCLASS + 1), s) != cudaSuccess) return PG_ECUDA;
+    k_tet_geometry<<<nblk, 128, 0, s>>>(p, ni, cls, hist);
+    k_class_offsets<<<1, 32, 0, s>>>(hist, cursor);
+    k_class_scatter<<<nblk, 128, 0, s>>>(cls, ni, cursor, order);
+    const long long nt = ni * p.nomc;
+    k_tet_eval<<<(unsigned)((nt + 127) / 128), 128, 0, s>>>(p, ni, cls);
+    pg_count_launches(4);
+  }
+  return PG_OK;
+}
+
+static Params make_params(const double* enk, int nbnd, int nkp, double ef, const int* kqid, int ncg, int numin,
+                          int nb1, int nb2, const double* omega, const int* tetc, int ntet, double* scratch,
+                          unsigned* d_status, unsigned long long* d_counters) {
+  Params p;
+  memset(&p, 0, sizeof(p));
+  p.enk = enk; p.kqid = kqid; p.omega = omega; p.tetc = tetc; p.scratch = scratch;
+  p.status = d_status; p.counters = d_counters; p.ef = ef;
+  p.nbnd = nbnd; p.nkp = nkp; p.ncg = ncg; p.numin = numin; p.nb1 = nb1; p.nb2 = nb2; p.ntet = ntet;
+  return p;
 }
 
 extern "C" size_t pg_bz_calcqdepw_par2_workspace(int nbnd, int nkp, int ncg, int nomx, int numin, int nom, int ntet,
@@ -1196,60 +1309,49 @@ extern "C" size_t pg_bz_calcqdepw_par2_workspace(int nbnd, int nkp, int ncg, int
   const long long nb1 = ncg + nomx + 1, nb2 = nbnd - ncg - numin;
   if (nb1 <= 0 || nb2 <= 0 || nkp <= 0 || ntet <= 0 || nom <= 0) return 0;
   const int nomc = (nom_chunk > 0 && nom_chunk < nom) ? nom_chunk : nom;
-  size_t b = lists_bytes(nkp, ntet, nb1 * nb2 * ntet);
-  b += align256(sizeof(double) * (size_t)4 * ntet * nomc * nb1 * nb2);
-  return b;
+  return weights_layout(nkp, ntet, nb1 * nb2, nomc, 0, REC_BUDGET).total;
 }
 
-extern "C" int pg_bz_calcqdepw_par2(const double* enk, int nbnd, int nkp, double ef, const int* kqid, int ncg,
-                                    int nomx, int numin, const double* omega, int nom, const int* tetc, int ntet,
-                                    double* kcw, void* work, size_t work_bytes, int nom_chunk, unsigned* d_status,
-                                    unsigned long long* d_counters, void* stream) {
+static int par2_impl(const double* enk, int nbnd, int nkp, double ef, const int* kqid, int ncg, int nomx, int numin,
+                     const double* omega, int nom, const int* tetc, int ntet, double* kcw, void* work,
+                     size_t work_bytes, int nom_chunk, size_t rec_budget, unsigned* d_status,
+                     unsigned long long* d_counters, void* stream) {
   const int nb1 = ncg + nomx + 1, nb2 = nbnd - ncg - numin;
   if (!enk || !kqid || !omega || !tetc || !kcw || !work) return PG_EARG;
   if (nb1 <= 0 || nb2 <= 0 || nkp <= 0 || ntet <= 0 || nom <= 0 || ncg < 0 || numin < 0) return PG_EARG;
   if (ntet != 6 * nkp) return PG_EARG;   // tetln = 6*kqid(ik)+it needs six tetrahedra per point
   const long long items = (long long)nb1 * nb2 * ntet;
   if (items >= (1ll << 31)) return PG_ETOOBIG;   // item indices are int
-  int nomc = (nom_chunk > 0 && nom_chunk < nom) ? nom_chunk : nom;
-  if (work_bytes < pg_bz_calcqdepw_par2_workspace(nbnd, nkp, ncg, nomx, numin, nom, ntet, nomc)) return PG_EWORKSPACE;
+  const int nomc = (nom_chunk > 0 && nom_chunk < nom) ? nom_chunk : nom;
+  const WLayout L = weights_layout(nkp, ntet, (long long)nb1 * nb2, nomc, 0, rec_budget);
+  if (work_bytes < L.total) return PG_EWORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
   char* w = (char*)work;
-  int* kptr = (int*)w; w += align256(sizeof(int) * (size_t)(nkp + 1));
-  int* kcount = (int*)w; w += align256(sizeof(int) * (size_t)nkp);
-  int* kslot = (int*)w; w += align256(sizeof(int) * (size_t)4 * ntet);
-  unsigned char* cls = (unsigned char*)w; w += align256((size_t)items);
-  int* order = (int*)w; w += align256(sizeof(int) * (size_t)items);
-  unsigned* hist = (unsigned*)w; w += align256(sizeof(unsigned) * NCLASS);
-  unsigned* cursor = (unsigned*)w; w += align256(sizeof(unsigned) * NCLASS);
-  double* scratch = (double*)w;
-  k_kcsr_count<<<(nkp + 127) / 128, 128, 0, s>>>(tetc, ntet, nkp, kcount);
-  k_kcsr_scan<<<1, 1, 0, s>>>(kcount, nkp, kptr);
-  k_kcsr_fill<<<(nkp + 127) / 128, 128, 0, s>>>(tetc, ntet, nkp, kptr, kslot);
+  double* scratch = (double*)(w + L.scratch);
+  enqueue_kcsr(L, w, tetc, ntet, nkp, s);
   const int P = nb1 * nb2;
-  const double wtet = 1.0 / ntet;
-  Params p;
-  p.enk = enk; p.kqid = kqid; p.omega = omega; p.tetc = tetc; p.scratch = scratch; p.order = nullptr;
-  p.status = d_status; p.counters = d_counters; p.ef = ef;
-  p.nbnd = nbnd; p.nkp = nkp; p.ncg = ncg; p.numin = numin; p.nb1 = nb1; p.nb2 = nb2; p.ntet = ntet;
-  p.om0 = 0; p.nomc = nomc;
-  // Sort the items by polyhedron class (frequency-independent, once per call).
-  const unsigned nblk = (unsigned)((items + 127) / 128);
-  if (cudaMemsetAsync(hist, 0, sizeof(unsigned) * NCLASS, s) != cudaSuccess) return PG_ECUDA;
-  k_tet_classify<<<nblk, 128, 0, s>>>(p, items, cls, hist);
-  k_class_offsets<<<1, 32, 0, s>>>(hist, cursor);
-  k_class_scatter<<<nblk, 128, 0, s>>>(cls, items, cursor, order);
-  pg_count_launches(6);
-  p.order = order;
+  Params p = make_params(enk, nbnd, nkp, ef, kqid, ncg, numin, nb1, nb2, omega, tetc, ntet, scratch, d_status,
+                         d_counters);
   for (int om0 = 0; om0 < nom; om0 += nomc) {
-    p.om0 = om0; p.nomc = (om0 + nomc <= nom) ? nomc : (nom - om0);
-    k_tet_weights<<<nblk, 128, 0, s>>>(p);
+    p.om0 = om0;
+    p.nomc = (om0 + nomc <= nom) ? nomc : (nom - om0);
+    const int rc = enqueue_tet_weights(p, L, w, s);
+    if (rc != PG_OK) return rc;
     dim3 g((P + 127) / 128, nkp, p.nomc);
-    k_gather<<<g, 128, 0, s>>>(scratch, kptr, kslot, P, nkp, p.nomc, om0, wtet, kcw);
-    pg_count_launches(2);
+    k_gather<<<g, 128, 0, s>>>(scratch, (const int*)(w + L.kptr), (const int*)(w + L.kslot), P, nkp, p.nomc, om0,
+                               1.0 / ntet, kcw);
+    pg_count_launches(1);
   }
   cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? PG_OK : PG_ECUDA;
+}
+
+extern "C" int pg_bz_calcqdepw_par2(const double* enk, int nbnd, int nkp, double ef, const int* kqid, int ncg,
+                                    int nomx, int numin, const double* omega, int nom, const int* tetc, int ntet,
+                                    double* kcw, void* work, size_t work_bytes, int nom_chunk, unsigned* d_status,
+                                    unsigned long long* d_counters, void* stream) {
+  return par2_impl(enk, nbnd, nkp, ef, kqid, ncg, nomx, numin, omega, nom, tetc, ntet, kcw, work, work_bytes,
+                   nom_chunk, REC_BUDGET, d_status, d_counters, stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -1258,8 +1360,7 @@ extern "C" size_t pg_bz_calcqdepw_par3_workspace(int nbnd, int nkp, int ncg, int
                                                   int nl) {
   const long long nb1 = ncg + nomx + 1, nb2 = nbnd - ncg - numin;
   if (nb1 <= 0 || nb2 <= 0 || nkp <= 0 || ntet <= 0 || nom <= 0 || nl <= 0) return 0;
-  return lists_bytes(nkp, ntet, nb1 * nb2 * ntet) + align256(sizeof(double) * (size_t)4 * ntet * nom * nb1 * nb2) +
-         align256(sizeof(double) * (size_t)4 * ntet * nl * nb1 * nb2);
+  return weights_layout(nkp, ntet, nb1 * nb2, nom, nl, REC_BUDGET).total;
 }
 
 // kcw (nb1, nb2, nkp, nl) = the par2 corner weights of every (tetrahedron,
@@ -1276,40 +1377,27 @@ extern "C" int pg_bz_calcqdepw_par3(const double* enk, int nbnd, int nkp, double
   if ((size_t)nom * nl * sizeof(double) > 48 * 1024) return PG_ETOOBIG;   // dUl staged in shared memory
   const long long items = (long long)nb1 * nb2 * ntet;
   if (items >= (1ll << 31)) return PG_ETOOBIG;
-  if (work_bytes < pg_bz_calcqdepw_par3_workspace(nbnd, nkp, ncg, nomx, numin, nom, ntet, nl)) return PG_EWORKSPACE;
+  const int P = nb1 * nb2;
+  const WLayout L = weights_layout(nkp, ntet, P, nom, nl, REC_BUDGET);
+  if (work_bytes < L.total) return PG_EWORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
   char* w = (char*)work;
-  int* kptr = (int*)w; w += align256(sizeof(int) * (size_t)(nkp + 1));
-  int* kcount = (int*)w; w += align256(sizeof(int) * (size_t)nkp);
-  int* kslot = (int*)w; w += align256(sizeof(int) * (size_t)4 * ntet);
-  unsigned char* cls = (unsigned char*)w; w += align256((size_t)items);
-  int* order = (int*)w; w += align256(sizeof(int) * (size_t)items);
-  unsigned* hist = (unsigned*)w; w += align256(sizeof(unsigned) * NCLASS);
-  unsigned* cursor = (unsigned*)w; w += align256(sizeof(unsigned) * NCLASS);
-  double* scratch = (double*)w; w += align256(sizeof(double) * (size_t)4 * ntet * nom * nb1 * nb2);
-  double* scratch2 = (double*)w;
-  k_kcsr_count<<<(nkp + 127) / 128, 128, 0, s>>>(tetc, ntet, nkp, kcount);
-  k_kcsr_scan<<<1, 1, 0, s>>>(kcount, nkp, kptr);
-  k_kcsr_fill<<<(nkp + 127) / 128, 128, 0, s>>>(tetc, ntet, nkp, kptr, kslot);
-  const int P = nb1 * nb2;
-  Params p;
-  p.enk = enk; p.kqid = kqid; p.omega = omega; p.tetc = tetc; p.scratch = scratch; p.order = nullptr;
-  p.status = d_status; p.counters = d_counters; p.ef = ef;
-  p.nbnd = nbnd; p.nkp = nkp; p.ncg = ncg; p.numin = numin; p.nb1 = nb1; p.nb2 = nb2; p.ntet = ntet;
-  p.om0 = 0; p.nomc = nom;
-  const unsigned nblk = (unsigned)((items + 127) / 128);
-  if (cudaMemsetAsync(hist, 0, sizeof(unsigned) * NCLASS, s) != cudaSuccess) return PG_ECUDA;
-  k_tet_classify<<<nblk, 128, 0, s>>>(p, items, cls, hist);
-  k_class_offsets<<<1, 32, 0, s>>>(hist, cursor);
-  k_class_scatter<<<nblk, 128, 0, s>>>(cls, items, cursor, order);
-  p.order = order;
-  k_tet_weights<<<nblk, 128, 0, s>>>(p);
+  double* scratch = (double*)(w + L.scratch);
+  double* scratch2 = (double*)(w + L.scratch2);
+  enqueue_kcsr(L, w, tetc, ntet, nkp, s);
+  Params p = make_params(enk, nbnd, nkp, ef, kqid, ncg, numin, nb1, nb2, omega, tetc, ntet, scratch, d_status,
+                         d_counters);
+  p.om0 = 0;
+  p.nomc = nom;
+  const int rc = enqueue_tet_weights(p, L, w, s);
+  if (rc != PG_OK) return rc;
   const long long nthr = (long long)4 * ntet * P;
   k_svd_project<<<(unsigned)((nthr + 127) / 128), 128, (size_t)nom * nl * sizeof(double), s>>>(
       scratch, dUl, nom, nl, P, (long long)4 * ntet, scratch2);
   dim3 g((P + 127) / 128, nkp, nl);
-  k_gather<<<g, 128, 0, s>>>(scratch2, kptr, kslot, P, nkp, nl, 0, 1.0 / ntet, kcw);
-  pg_count_launches(10);
+  k_gather<<<g, 128, 0, s>>>(scratch2, (const int*)(w + L.kptr), (const int*)(w + L.kslot), P, nkp, nl, 0,
+                             1.0 / ntet, kcw);
+  pg_count_launches(2);
   cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? PG_OK : PG_ECUDA;
 }
@@ -1382,11 +1470,16 @@ extern "C" int pg_bz_calcqdepw_par2_noalloc(const double* enk, int nbnd, int nkp
   if (!enk || !kqid || !omega || !tetc || !kcw) return PG_EARG;
   if (nb1 <= 0 || nb2 <= 0 || nkp <= 0 || ntet <= 0 || nom <= 0 || ncg < 0 || numin < 0) return PG_EARG;
   if (ntet != 6 * nkp) return PG_EARG;
-  // Largest frequency chunk whose scratch fits next to the k lists and the item order.
-  const size_t lists = lists_bytes(nkp, ntet, (long long)nb1 * nb2 * ntet);
-  const size_t per_omega = sizeof(double) * (size_t)4 * ntet * (size_t)nb1 * nb2;
-  if (lists + per_omega + 256 > (size_t)PG_NOALLOC_SCRATCH_BYTES) return PG_ETOOBIG;
-  const size_t fit = ((size_t)PG_NOALLOC_SCRATCH_BYTES - lists - 256) / per_omega;
+  // A quarter of the array for the sub-tetrahedron records of one
+  // tetrahedron chunk, and the largest frequency chunk whose scratch fits in
+  // the rest next to the k lists and the item arrays.
+  const long long P = (long long)nb1 * nb2;
+  const size_t cap = (size_t)PG_NOALLOC_SCRATCH_BYTES, rec_budget = cap / 4;
+  if ((long long)P * ntet >= (1ll << 31)) return PG_ETOOBIG;
+  const size_t fixed = weights_layout(nkp, ntet, P, 0, 0, rec_budget).total;
+  const size_t per_omega = sizeof(double) * (size_t)4 * ntet * (size_t)P;
+  if (fixed + per_omega + 256 > cap) return PG_ETOOBIG;
+  const size_t fit = (cap - fixed - 256) / per_omega;
   const int nomc = (int)((fit < (size_t)nom) ? fit : (size_t)nom);
   // Lookup of the array's device address once per device context: in host
   // code the symbol names a host-side stand-in, not device memory.
@@ -1404,6 +1497,6 @@ extern "C" int pg_bz_calcqdepw_par2_noalloc(const double* enk, int nbnd, int nkp
     }
     base = g_noalloc_ptr[dev];
   }
-  return pg_bz_calcqdepw_par2(enk, nbnd, nkp, ef, kqid, ncg, nomx, numin, omega, nom, tetc, ntet, kcw, base,
-                              (size_t)PG_NOALLOC_SCRATCH_BYTES, nomc, d_status, d_counters, stream);
+  return par2_impl(enk, nbnd, nkp, ef, kqid, ncg, nomx, numin, omega, nom, tetc, ntet, kcw, base, cap, nomc,
+                   rec_budget, d_status, d_counters, stream);
 }
