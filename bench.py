@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="C3")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--prep-batch", type=int, default=0,
+                    help="split-precision chi0: frequencies per B-digit preparation pass (0: the library default)")
     ap.add_argument("--fp64-k-sample", type=int, default=4,
                     help="k-points on which the plain FP64 GPU contraction is timed for the comparison line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -297,13 +299,18 @@ MEASURED_GEMM_TRAFFIC = {
 }
 
 
-# FP64 work of the weights kernel and the FP64 ceiling it is held to, from one
-# ncu capture of k_tet_weights and k_chi0_f64 (thread-level dadd + dmul + 2·dfma
-# instruction counts, gpu__time_duration): (FP64 flops of k_tet_weights per
-# (sub-tetrahedron, ω) evaluation — geometry included — counted by its exact +
-# Taylor counters; k_chi0_f64's FP64 rate in TFLOP/s, the FP64 pipe then being
-# nearly saturated; where the capture is summarised).
-WEIGHTS_FP64 = (614.8, 1.212, "profiles/fp64_work_k_tet_weights_k_chi0_f64_c2_div4.md")
+# FP64 work of the weight kernels and the FP64 ceiling it is held to, from one
+# ncu capture of k_tet_geometry, k_tet_eval and k_chi0_f64 (thread-level dadd,
+# dmul, dfma instruction counts, FP64-pipe instructions, gpu__time_duration):
+# (FP64 flops (dadd + dmul + 2·dfma) per (sub-tetrahedron, ω) evaluation,
+# geometry included, counted by the kernels' exact + Taylor counters;
+# k_chi0_f64's FP64 rate in TFLOP/s with its FP64 pipe 97 % busy; FP64-pipe
+# thread instructions per evaluation (flop-type and the rest: comparisons,
+# conversions); k_chi0_f64's FP64-pipe thread-instruction rate; where the
+# capture is summarised).  The weights mix single-flop adds and multiplies
+# and non-flop FP64 instructions into their FMAs, so they keep the FP64 pipe
+# busy at a lower flop rate than the FMA-only contraction.
+WEIGHTS_FP64 = (308.9, 1.212, 316.0, 0.6112e12, "profiles/fp64_work_k_tet_geometry_eval_k_chi0_f64_c2_div4.md")
 
 
 def measure_accuracy(inp):
@@ -347,20 +354,25 @@ def weights_roofline(inp):
     kcw_bytes = 8 * inp.nb1 * inp.nb2 * inp.nkp * nom
     hbm = json.load(open(PEAKS_FILE)).get("hbm_gbs") if os.path.exists(PEAKS_FILE) else 6800.0
     gbs = kcw_bytes / (t_ms * 1e-3) / 1e9
-    out = {"kernel": "weights phase (k_tet_classify, k_class_scatter, k_tet_weights, k_gather, k lists)",
+    out = {"kernel": "weights phase (k lists, k_tet_geometry, k_class_scatter, k_tet_eval, k_gather)",
            "phase_ms": t_ms, "evaluations": {"exact": c["exact"], "taylor": c["taylor"], "calls": c["calls"]},
            "hbm": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
                    "algorithmic_bytes": kcw_bytes, "note": "kcw written (8 B per band pair, k-point, frequency) / "
                                                           "phase time; peak = measured copy bandwidth"},
            "fp64": None}
     if WEIGHTS_FP64 is not None:
-        per_eval, ceiling, src = WEIGHTS_FP64
-        flops = per_eval * (c["exact"] + c["taylor"])
+        per_eval, ceiling, instr_per_eval, instr_ceiling, src = WEIGHTS_FP64
+        nev = c["exact"] + c["taylor"]
+        flops = per_eval * nev
         tf = flops / (t_ms * 1e-3) / 1e12
+        ips = instr_per_eval * nev / (t_ms * 1e-3)
         out["fp64"] = {"bound": "fp64", "achieved": tf, "peak": ceiling, "unit": "TFLOP/s", "frac": tf / ceiling,
                        "flops": flops, "source": src,
-                       "note": "FP64 flops = per-evaluation count x (exact + Taylor evaluations of this q); "
-                               "peak = FP64 rate of this build's k_chi0_f64 (FP64 pipe near saturation)"}
+                       "pipe_frac": ips / instr_ceiling,
+                       "note": "FP64 flops = per-evaluation count (dadd + dmul + 2 dfma) x (exact + Taylor "
+                               "evaluations of this q); peak = FP64 rate of this build's k_chi0_f64 (FP64 pipe "
+                               "97 % busy); pipe_frac = FP64-pipe instructions per evaluation x evaluations / "
+                               "phase time / k_chi0_f64's FP64-pipe instruction rate"}
     return out
 
 
@@ -798,6 +810,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from pygw_gb300 import _lib
+    _lib.check(_lib.load().pg_set_chi0_prep_batch(a.prep_batch), "pg_set_chi0_prep_batch")
 
     if a.path == "selfc":
         return run_selfc(a, w, rank, world, sampler)
@@ -944,6 +957,7 @@ def main():
                 "vs_baseline": None, "dtype": "f64" if a.precision == "fp64" else "bf16-digits/f32-exact/f64",
                 "data": "synthetic",
                 "config": {"workload": workload_desc(w), "precision": a.precision, "parallelism": "replicas",
+                           "chi0_prep_batch": lib.pg_chi0_prep_batch() if a.precision == "mixed" else None,
                            "l2": "inputs larger than L2 (matrix elements %.2f GB read every step)"
                                  % (inp.minm_host.numel() * 16 / 1e9)},
                 "roofline": roof, "roofline_weights": roof_w, "accuracy": acc, "kernel_status": status_bits,

@@ -249,7 +249,9 @@ class Batch:
                                                    ptr(self.cwork), self.cwork.numel(), wb, 0,
                                                    ptr(self.cstatus[i:i + 1]), sh, None)
             self._check(rc, "pg_chi0_mixed_accumulate")
-            if i in self.q0 and eps is self.results[i]:
+            # the wings belong to the batch's own result (not to a tuning probe,
+            # which runs before the results exist)
+            if i in self.q0 and eps is getattr(self, "results", [None] * (i + 1))[i]:
                 q = self.q0[i]
                 rc = self.lib.pg_wings_f64(ptr(mv), kc, k0, ptr(self.kcw), self.nb1, self.nb2, self.nkp, nom, N,
                                            -FSPIN, ptr(q["pm"][k0:k0 + kc]), ptr(q["w1"]), sh)

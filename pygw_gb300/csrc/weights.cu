@@ -4,22 +4,29 @@
 // callees (for_tetrahedra3.f90:3-743, for_tetrahedra2.f90:1688-2773).
 //
 // Structure (GPU-first, deterministic):
-//   1. k_kcsr_*     : for every mesh point k, the ascending list of
-//                     (tetrahedron, corner) slots that touch it (CSR).
-//   2. k_tet_weights: one thread per (tetrahedron, occupied band ib,
-//                     unoccupied band jb).  It builds the integration polyhedron
-//                     {e ≤ EF ≤ f} (surfnodes → unrepnodes → relnodes →
-//                     sortnodes), splits it into sub-tetrahedra and evaluates
-//                     the closed-form corner weights with all Matsubara points
-//                     in the innermost loop.  atan/log are evaluated once per
-//                     distinct corner value and frequency (4 + 4 in the generic
-//                     case, where the reference evaluates 16 + 16) and shared by
-//                     the four vertex formulas.  Results go to a scratch array
-//                     laid out [tet][corner][ω][pair] so each warp store is
-//                     256 contiguous bytes.
-//   3. k_gather     : kcw[pair, k, ω] = Σ over k's CSR slots in ascending
-//                     tetrahedron order of (w·6)·(1/ntet) — the reference's
-//                     accumulation order, without atomics.
+//   1. k_kcsr_*       : for every mesh point k, the ascending list of
+//                       (tetrahedron, corner) slots that touch it (CSR).
+//   Then per chunk of tetrahedra (items = (tetrahedron, occupied band ib,
+//   unoccupied band jb)):
+//   2. k_tet_geometry : one thread per item.  It builds the integration
+//                       polyhedron {e ≤ EF ≤ f} (surfnodes → unrepnodes →
+//                       relnodes → sortnodes), splits it into sub-tetrahedra
+//                       and sets each one up (volume, sorteq grouping,
+//                       closed-form coefficients): frequency-independent work,
+//                       done once and stored as records, with the item's
+//                       class (node count, first grouping).
+//   3. k_class_offsets / k_class_scatter: the chunk's items in class order.
+//   4. k_tet_eval     : one thread per (item, frequency) in class order: the
+//                       closed-form corner weights of the item's records at
+//                       that frequency.  atan/log are evaluated once per
+//                       distinct corner value (4 + 4 in the generic case, where
+//                       the reference evaluates 16 + 16) and shared by the four
+//                       vertex formulas.  Lanes of a warp share one item (and
+//                       its code path); the kernel has no stack frame.  Results
+//                       go to a scratch array laid out [tet][corner][ω][pair].
+//   5. k_gather       : kcw[pair, k, ω] = Σ over k's CSR slots in ascending
+//                       tetrahedron order of (w·6)·(1/ntet) — the reference's
+//                       accumulation order, without atomics.
 //
 // Arithmetic matches the oracle bit for bit: this file is compiled with
 // -fmad=false, atan/log come from fp64_math.h, and every expression keeps the

@@ -42,6 +42,21 @@ class EpsResult:
                 self.head.cpu().numpy().copy())
 
 
+_COPY_STREAMS: dict[int, "torch.cuda.Stream"] = {}
+
+
+def _copy_stream():
+    """One host→device copy stream per device for the life of the process:
+    the caching allocator keeps blocks per stream, so a fresh stream per call
+    would allocate (and eventually release, synchronising) the staged matrix
+    elements anew every call."""
+    dev = torch.cuda.current_device()
+    st = _COPY_STREAMS.get(dev)
+    if st is None:
+        st = _COPY_STREAMS[dev] = torch.cuda.Stream(device=dev)
+    return st
+
+
 def _kcw_device(kcw):
     """kcw as a CUDA float64 tensor whose storage is the Fortran order of (nb1, nb2, nkp, nom)."""
     if isinstance(kcw, torch.Tensor):
@@ -141,7 +156,7 @@ def chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=None, k_chunk=Non
         return eps, epsw1
 
     if staged:
-        copy_stream = torch.cuda.Stream()
+        copy_stream = _copy_stream()
         # allocated on the copy stream: its memory is none that kernels still
         # queued on the compute stream use, so the copy need not wait for them
         with torch.cuda.stream(copy_stream):
@@ -159,7 +174,7 @@ def chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=None, k_chunk=Non
         # pinned host tensor: double-buffered H2D on a copy stream
         m = minm.reshape(nkp, P, npb)
         bufs = [torch.empty((k_chunk, P, npb), dtype=torch.complex128, device="cuda") for _ in range(2)]
-        copy_stream = torch.cuda.Stream()
+        copy_stream = _copy_stream()
         # The buffers come from the caching allocator of the compute stream and
         # may reuse memory that kernels still queued there (e.g. the weight
         # kernel's workspace) are using: the copy stream starts after them, and

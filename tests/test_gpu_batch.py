@@ -62,7 +62,8 @@ def test_batch_q0_wings_and_head_match_oracle():
     b = prob.bands
     tasks = pb.c5_tasks(prob)
     assert tasks[0].iq == 0 and tasks[0].pm is not None
-    bt = pb.batch_for(prob, tasks)
+    # tuned: the tuner's probes of the q = Γ task run before the results exist
+    bt = pb.batch_for(prob, tasks, tuner=pb.Tuner(probe_nom=2))
     bt.run(graph=True)
     assert bt.status() == 0
     nomx, numin = b.nomax_numin
