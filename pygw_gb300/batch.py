@@ -35,7 +35,7 @@ import torch
 
 from . import _lib
 from . import eps as peps
-from .device import ptr, require_cuda, stream_handle
+from .device import free_device_bytes, ptr, require_cuda, stream_handle
 
 FSPIN = 2.0
 
@@ -125,7 +125,7 @@ class Batch:
         self.sqv_d = [torch.from_numpy(np.asarray(t.sqv, dtype=np.float64)).cuda() for t in self.tasks]
         self.kcw = torch.empty((self.nom, self.nkp, self.nb2, self.nb1), dtype=torch.float64, device="cuda")
         # weight scratch: all frequencies at once unless that exceeds a quarter of the free memory
-        free0, _ = torch.cuda.mem_get_info()
+        free0 = free_device_bytes()
         self.nom_chunk = self.nom
         while self.nom_chunk > 1 and self.lib.pg_bz_calcqdepw_par2_workspace(
                 self.nbnd, self.nkp, ncg, nomx, numin, self.nom, self.ntet, self.nom_chunk) > free0 // 4:
@@ -154,7 +154,7 @@ class Batch:
                      else np.minimum(np.asarray(t.knb2, dtype=np.int32), self.nb2) for t in self.tasks]
         self.ktot = [int(self.nb1 * kn.sum()) for kn in self.knb2]
         # tuning (before any buffer sized by the choice is allocated)
-        free, _ = torch.cuda.mem_get_info()
+        free = free_device_bytes()
         results_bytes = sum(16 * self.nom * t.npb * t.npb for t in self.tasks)
         eps_ws = max(self.lib.pg_eps_inverse_mixed_workspace(t.npb, self.nom, 0) for t in self.tasks)
         self.budget = max(1 << 28, int(mem_fraction * free) - results_bytes - eps_ws)

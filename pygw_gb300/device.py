@@ -35,3 +35,12 @@ def to_device(a, dtype=None):
 
 def workspace(nbytes: int):
     return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device="cuda")
+
+
+def free_device_bytes() -> int:
+    """Device memory a new allocation can use: what the driver reports free
+    plus what PyTorch's caching allocator holds reserved but unused (after a
+    large call the allocator keeps its blocks, which the driver counts as in
+    use; sizing the next call on the driver's figure alone would shrink it)."""
+    free, _ = torch.cuda.mem_get_info()
+    return int(free + torch.cuda.memory_reserved() - torch.cuda.memory_allocated())

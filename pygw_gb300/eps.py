@@ -19,7 +19,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .device import ptr, require_cuda, stream_handle, to_device, workspace
+from .device import free_device_bytes, ptr, require_cuda, stream_handle, to_device, workspace
 
 PRECISION = "fp64"      # 'fp64' (plain comparator) or 'mixed' (split-precision tensor-core χ0)
 FSPIN = 2.0
@@ -125,7 +125,7 @@ def chi0_accumulate(kcw_d, minm, nkp, npb, nb1, nb2, nom, pm_k=None, k_chunk=Non
     # the digit preparation and run shorter GEMM launches).
     staged = False
     if not on_device and k_chunk is None and precision == "mixed" and isinstance(minm, torch.Tensor):
-        free, _ = torch.cuda.mem_get_info()
+        free = free_device_bytes()
         wb_all = mixed_omega_batch(nb1, nb2, nkp, npb, nom)
         need = nkp * P * npb * 16 + lib.pg_chi0_mixed_workspace(nb1, nb2, nkp, npb, wb_all, 0)
         staged = need <= 0.8 * free
@@ -238,7 +238,7 @@ def mixed_omega_batch(nb1, nb2, nkp, npb, nom, budget_bytes=None, sm_count=None)
     current device's."""
     lib = _lib.load()
     if budget_bytes is None:
-        free, _ = torch.cuda.mem_get_info()
+        free = free_device_bytes()
         budget_bytes = int(0.4 * free)
     if sm_count is None:
         sm_count = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
@@ -322,7 +322,7 @@ def eps_inverse_batch(npb, nom, budget_bytes=None):
     budget (default: 30 % of the free device memory)."""
     lib = _lib.load()
     if budget_bytes is None:
-        free, _ = torch.cuda.mem_get_info()
+        free = free_device_bytes()
         budget_bytes = int(0.3 * free)
     nb = nom
     while nb > 1 and lib.pg_eps_inverse_mixed_workspace(npb, nom, nb) > budget_bytes:
