@@ -183,6 +183,27 @@ def test_chi0_prep_batch_setting():
     assert lib.pg_chi0_prep_batch() == 4 and lib.pg_chi0_mixed_workspace(*args) == base
 
 
+def test_weights_workspace_holds_scratch_and_records():
+    """The weights workspace (host arithmetic): the scratch weights grow by
+    4·ntet·P doubles per frequency of the chunk, and next to them sit the k
+    lists, the per-chunk item arrays and the sub-tetrahedron records of one
+    tetrahedron chunk (at most 1 GiB, at least one tetrahedron's worth: six
+    records per band pair)."""
+    from pygw_gb300 import _lib
+    lib = _lib.load()
+    nbnd, nkp, ncg, nomx, numin, nom, ntet = 200, 216, 0, 22, 8, 48, 1296     # C3: 23 × 192 band pairs
+    P = (ncg + nomx + 1) * (nbnd - ncg - numin)
+    per_omega = 4 * ntet * P * 8
+    ws = [lib.pg_bz_calcqdepw_par2_workspace(nbnd, nkp, ncg, nomx, numin, nom, ntet, c) for c in (1, 2, 48)]
+    assert ws[1] - ws[0] == per_omega and ws[2] - ws[0] == 47 * per_omega
+    rest = ws[0] - per_omega
+    assert 6 * P * 800 < rest <= (1 << 30) + (64 << 20)
+    assert lib.pg_bz_calcqdepw_par2_workspace(nbnd, nkp, ncg, nomx, numin, nom, ntet, 0) == ws[2]
+    # a small problem: the records of all its tetrahedra fit in one chunk
+    small = lib.pg_bz_calcqdepw_par2_workspace(10, 8, 0, 3, 2, 4, 48, 0)
+    assert 4 * 48 * 32 * 4 * 8 < small < 4 * 48 * 32 * 4 * 8 + 48 * 32 * 6 * 1024 + (1 << 16)
+
+
 def test_polarization_entry_points_validate_on_the_host():
     """The weights, χ0 and ε⁻¹ entry points reject null pointers, inconsistent
     sizes and short workspaces before any device call (host code: runs without
