@@ -59,3 +59,23 @@ def test_scaled_digit_step_gives_the_digits_of_the_two_sum_step():
             assert np.array_equal(d0, d1)
             assert np.array_equal(np.signbit(d0), np.signbit(d1))
             assert np.all(np.abs(d0) <= 256)
+
+
+def test_accumulator_split_by_add_subtract_equals_rint():
+    """The digit GEMM's drain moves the nearest multiple of 2^12 of each FP32
+    accumulator value v (an integer, |v| < 2^24) into a register accumulator.
+    It rounds by two additions, (v + 1.5·2^35) − 1.5·2^35: v + 1.5·2^35 lies in
+    [2^35, 2^36), where the float32 spacing is 2^12, so the first addition
+    rounds v to that spacing (ties to even) and the second is exact.  Checked
+    against rint(v·2^-12)·2^12 on random integers, on every tie and on the
+    range ends."""
+    rng = np.random.default_rng(7)
+    v = rng.integers(-(1 << 24) + 1, 1 << 24, size=2_000_000).astype(f32)
+    ties = (np.arange(-(1 << 12), 1 << 12, dtype=np.int64) * 4096 + 2048)
+    ends = np.array([0, 1, -1, 2047, 2048, 2049, -2048, (1 << 24) - 1, -(1 << 24) + 1], dtype=np.int64)
+    v = np.concatenate([v, ties.astype(f32), ends.astype(f32)])
+    c = f32(1.5 * 2.0 ** 35)
+    hh = (v + c) - c
+    assert np.array_equal(hh, np.rint(v * f32(1.0 / 4096)) * f32(4096))
+    r = v - hh
+    assert np.all(np.abs(r) <= 2048) and np.array_equal(hh + r, v)
