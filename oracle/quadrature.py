@@ -1,9 +1,8 @@
 """Independent quadrature of the tetrahedron weight integral (test infrastructure).
 
-Parity unpinned: the reference ships no tests, fixtures or golden vectors for this
-path and cannot be built or run here (Fortran without a compiler, Python 2 with
-f2py modules); this restatement is pinned by known answers instead
-(tests/test_oracle_*.py).
+A numerical integral of the same integrand, independent of the closed forms
+(the reference's and the oracle's): tests/test_oracle_weights.py checks the
+oracle against it.
 
 Restates the integrand of ``stweight_numeric`` (for_tetrahedra2.f90:1504-1604,
 ``iop_omg = 1``): for the unit tetrahedron with energy differences ``de`` at

@@ -1,8 +1,14 @@
 // ORACLE — test infrastructure only, never part of the product path.
 //
-// Parity unpinned: the reference ships no tests, fixtures or golden vectors for
-// this path and its Fortran cannot be built here (no Fortran compiler); this
-// restatement is pinned by known answers instead (tests/test_oracle_weights.py).
+// Parity pinned against the reference's own statements: the reference ships no
+// tests or golden vectors for this path and no Fortran compiler exists here, so
+// tests/golden/make_weights_golden.py executes bz_calcqdepw_par2 and its callees
+// from their Fortran text (tests/golden/f90py.py, kinds and storage association
+// kept) on seeded inputs; this restatement reproduces those kcw bit for bit
+// with either atan/log (tests/test_oracle_weights_golden.py), except where the
+// reference's wtemp(4,2,nom) layout aliases the halves of 7- and 8-node
+// polyhedra from the third frequency on (see convw1t below).  Known answers
+// (tests/test_oracle_weights.py) check the integrals themselves.
 //
 // CPU restatement of PyGW's imaginary-axis tetrahedron polarization weights
 // (the routine PyGW calls as ft.bz_calcqdepw_par2, pygw.py:3443), written to
@@ -21,12 +27,6 @@
 //   unrepnodes          for_tetrahedra2.f90:2116-2175
 //   relnodes / tlinap   for_tetrahedra2.f90:2177-2304
 //   sortnodes           for_tetrahedra2.f90:2306-2773
-//
-// Parity status: the Fortran cannot be compiled in this project's toolchains
-// (no Fortran compiler), and the reference ships no test vectors, so this
-// restatement is pinned by known answers instead (flat bands, Gauss–Legendre
-// quadrature of the same integral, Taylor/closed-form continuity,
-// permutation structure) — see tests/test_oracle_weights.py.
 //
 // Conventions where the reference is undefined (uninitialised locals, writes
 // through a zero index, bit tests at a garbage position): every such event
@@ -960,6 +960,13 @@ static void convw1t(double* weight, const double e[4], const double f[4], double
       break;
     case 7:
     case 8: {
+      // The two halves' weights, summed per frequency.  The reference keeps
+      // them in wtemp(4,2,nom) but addresses it as (4,nom,2)
+      // (for_tetrahedra3.f90:36, 100-120); as compiled code addresses that
+      // out-of-bounds layout, the second half overwrites the first from the
+      // third frequency on and frequency j >= 3 gets w2(j-2) + w2(j).  This
+      // restatement adds w1(j) + w2(j), which is what the reference computes
+      // for the first two frequencies and what its code evidently means.
       const int cap = (nnod == 7) ? 5 : 6;
       double w1[4 * NOM_MAX], w2[4 * NOM_MAX];
       for (int isub = 1; isub <= 2; isub++) {

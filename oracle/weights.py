@@ -1,9 +1,12 @@
 """ctypes front end of the oracle's weight restatement (test infrastructure).
 
-Parity unpinned: the reference ships no tests, fixtures or golden vectors for this
-path and cannot be built or run here (Fortran without a compiler, Python 2 with
-f2py modules); this restatement is pinned by known answers instead
-(tests/test_oracle_*.py).
+Parity pinned against the reference's own statements: with no Fortran compiler
+here, tests/golden/make_weights_golden.py executes the reference's
+bz_calcqdepw_par2 and its callees from their Fortran text (tests/golden/f90py.py)
+on seeded inputs, and this restatement reproduces those kcw bit for bit
+(tests/test_oracle_weights_golden.py) except at the reference's own layout bug
+for 7- and 8-node polyhedra (frequencies from the third on); known answers
+(tests/test_oracle_*.py) check the integrals themselves.
 
 ``bz_calcqdepw_par2`` mirrors the f2py call of the reference
 (``kcw = ft.bz_calcqdepw_par2(enk, ef, kqid, ncg, nomx, numin, omega, tetc)``,

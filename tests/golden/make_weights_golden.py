@@ -1,0 +1,111 @@
+"""Generate golden tetrahedron weights from the reference's own Fortran statements.
+
+Run where the reference's source tree is available:
+
+    python tests/golden/make_weights_golden.py --reference <PyGW source tree>
+
+Neither this container nor the GPU machine has a Fortran compiler, so the
+reference's ``bz_calcqdepw_par2`` (for_tetrahedra.f90:390-464) and everything
+it calls (``convw1t_par``, ``surfnodes`` … ``sortnodes``, ``generictetra_par``,
+``stweight_imag_par``, ``stweight_itaylor_par``, ``sorteq``: for_tetrahedra2.f90
+and for_tetrahedra3.f90) are read from the reference's files and executed
+statement by statement through ``f90py`` (beside this script), which keeps
+every variable's declared kind and passes arguments by reference with the
+storage association compiled Fortran uses.  The only substitution is the
+arc tangent and logarithm: each case is run twice, once with the C library's
+``atan``/``log`` (what a compiled reference calls) and once with the portable
+implementations the oracle and the GPU kernels share, so that the oracle's
+restatement can be compared bit for bit with the reference's statements.
+
+Cases (seeded synthetic band structures with the workload generator's
+shapes): C1-like bands on a 2³ k-mesh, and a stress case whose partially
+occupied bands give polyhedra with 5 to 8 nodes; four imaginary frequencies
+each.  Output: ``weights_golden.npz`` (inputs and the reference's ``kcw`` for
+each math variant); nothing of the reference's source is stored.
+"""
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+sys.path.insert(0, ROOT)
+import f90py  # noqa: E402
+from refsrc import reference_file  # noqa: E402
+
+OUT = os.path.join(HERE, "weights_golden.npz")
+FILES = ["for_tetrahedra.f90", "for_tetrahedra2.f90", "for_tetrahedra3.f90"]
+
+
+def reference_par2(math_impl):
+    atan, log = math_impl
+    procs, _ = f90py.load([reference_file(f) for f in FILES], ["bz_calcqdepw_par2"], atan, log)
+    fn = procs["bz_calcqdepw_par2"]
+
+    def run(enk, ef, kqid, ncg, nomx, numin, omega, tetc):
+        enk = np.asfortranarray(enk, dtype=np.float64)
+        tetc = np.asfortranarray(tetc, dtype=np.int32)
+        nbnd, nkp = enk.shape
+        ntet = tetc.shape[1]
+        nom = len(omega)
+        nb1, nb2 = ncg + nomx + 1, nbnd - ncg - numin
+        kcw = f90py.FArr(np.zeros((nb1, nb2, nkp, nom), order="F"), (1, 1, 1, 1))
+        i4 = lambda x: np.array(x, dtype=np.int32)     # noqa: E731
+        fn(kcw, f90py.FArr(enk, (1, 1)), np.array(float(ef)), f90py.FArr(np.asarray(kqid, dtype=np.int32).copy(), (1,)),
+           i4(ncg), i4(nomx), i4(numin), f90py.FArr(np.asarray(omega, dtype=np.float64).copy(), (1,)),
+           f90py.FArr(tetc, (1, 1)), i4(nkp), i4(nom), i4(nbnd), i4(ntet))
+        return kcw.a.copy()
+    return run
+
+
+def cases():
+    from pygw_gb300 import synthetic as syn
+    out = {}
+    # C1-like bands, 2³ k-mesh, the last q point
+    w = syn.scaled(syn.WORKLOADS["C1"], div=2, nbands=16, nocc=4, nom=4)
+    p = syn.Problem(w)
+    b = p.bands
+    nomx, numin = b.nomax_numin
+    iq = p.qs[-1]
+    out["c1"] = dict(enk=b.enk(), ef=b.EF, kqid=p.kqm.kqid[:, iq], ncg=0, nomx=nomx, numin=numin,
+                     omega=p.fr.omega, tetc=p.kqm.tetc)
+    # stress: bands crossing the Fermi level everywhere on the same mesh, so
+    # that the polyhedra {e <= EF <= f} take every node count
+    rng = np.random.default_rng(11)
+    nkp = p.kqm.nkp
+    occ = rng.uniform(-0.6, 0.4, (3, nkp))
+    emp = rng.uniform(-0.3, 0.9, (5, nkp))
+    enk = np.concatenate([np.sort(occ, axis=0), np.sort(emp, axis=0)])
+    out["stress"] = dict(enk=np.asfortranarray(enk), ef=0.0, kqid=p.kqm.kqid[:, iq], ncg=0, nomx=2, numin=0,
+                         omega=np.array([0.02, 0.2, 2.0, 20.0]), tetc=p.kqm.tetc)
+    return out
+
+
+def main():
+    from oracle import weights as ow
+
+    def portable_atan(x):
+        return float(ow.portable_math(np.array([x]))[0][0])
+
+    def portable_log(x):
+        return float(ow.portable_math(np.array([x]))[1][0])
+
+    variants = {"libm": (math.atan, math.log), "portable": (portable_atan, portable_log)}
+    store = {}
+    for name, c in cases().items():
+        for k, v in c.items():
+            store[f"{name}.{k}"] = np.asarray(v)
+        for vname, impl in variants.items():
+            run = reference_par2(impl)
+            kcw = run(c["enk"], c["ef"], c["kqid"], c["ncg"], c["nomx"], c["numin"], c["omega"], c["tetc"])
+            store[f"{name}.kcw_{vname}"] = kcw
+            print(f"{name} ({vname}): kcw {kcw.shape}, {np.count_nonzero(kcw)} nonzero", flush=True)
+    np.savez_compressed(OUT, **store)
+    print("wrote", OUT)
+
+
+if __name__ == "__main__":
+    main()
