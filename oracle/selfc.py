@@ -1,13 +1,14 @@
 """numpy restatement of the correlation self-energy contraction (test infrastructure).
 
-Pinned in two ways.  The Python parts of the reference — the mwm contraction
-with its q = 0 terms, the energies at k − q, the iopfreq 4 interpolation and
-the SVD-branch product — are checked against golden vectors from the
-reference's own calc_selfc and Compute_selfc_inside, run on seeded inputs by
-tests/golden/make_calc_selfc_golden.py (tests/test_oracle_selfc_golden.py).
-The Fortran convolution kernels (fnc.f90) cannot be built here (no Fortran
-compiler); their restatement below is pinned by known answers
-(tests/test_oracle_selfc.py).
+Pinned against the reference's own code: tests/golden/make_calc_selfc_golden.py
+runs the reference's calc_selfc and Compute_selfc_inside (Python) with the
+Fortran convolution kernels they call (fnc.f90, no compiler here) executed from
+their source text through tests/golden/f90py.py, complex division formed as
+compiled Fortran forms it; this restatement reproduces mwm, the energies at
+k − q, the iopfreq 4 interpolation and the SVD-branch product, and the
+convolutions to the last few bits (numpy's complex division rounds
+differently), within 1e-12 (tests/test_oracle_selfc_golden.py).  Known
+answers (tests/test_oracle_selfc.py) check the integrals themselves.
 
 Follows MatrixElements2Band.calc_selfc (pygw.py:3299-3412) for one q and the
 frequency convolution it calls (mcommon.py:80-131 → fnc.f90:90-177):

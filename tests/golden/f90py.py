@@ -44,7 +44,7 @@ class FortranStop(Exception):
 
 
 # ----------------------------------------------------------------- runtime
-I1, I4, I8, R4, R8, LG = np.int8, np.int32, np.int64, np.float32, np.float64, np.bool_
+I1, I4, I8, R4, R8, LG, C16 = np.int8, np.int32, np.int64, np.float32, np.float64, np.bool_, np.complex128
 
 
 class Sect:
@@ -175,7 +175,7 @@ def _base_and_offset(a):
     return base, off
 
 
-def assoc_array(actual, dtype, dims, lbs):
+def assoc_array(actual, dtype, dims, lbs, intent=None):
     """Dummy array of explicit shape ``dims`` (None = assumed, from the
     actual) with lower bounds ``lbs``, associated with ``actual``."""
     if isinstance(actual, ElemRef):
@@ -202,6 +202,12 @@ def assoc_array(actual, dtype, dims, lbs):
         flat = src.reshape(-1, order="F")
         if np.shares_memory(flat, src) or src.size == 0:
             return FArr(flat[:size].reshape(shape, order="F"), lbs)
+    if isinstance(actual, (FArr, np.ndarray)) and not src.flags.f_contiguous and intent == "in":
+        # a non-contiguous section to an intent(in) dummy: compiled code passes
+        # a contiguous copy (copy-in)
+        if src.size < size:
+            raise IndexError("dummy array larger than its actual argument")
+        return FArr(np.asfortranarray(src).reshape(-1, order="F")[:size].reshape(shape, order="F"), lbs)
     # sequence association from the first element on, through the storage of
     # the whole array the actual belongs to (column-major)
     base, off = _base_and_offset(first)
@@ -249,7 +255,61 @@ def _is_int(x):
     return np.issubdtype(np.asarray(x).dtype, np.integer)
 
 
+def _parts(x):
+    x = np.asarray(x)
+    if np.iscomplexobj(x):
+        return x.real.astype(np.float64), x.imag.astype(np.float64), True
+    return x.astype(np.float64), None, False
+
+
+def _mkc(re_, im):
+    re_ = np.asarray(re_, dtype=np.float64)
+    r = np.empty(re_.shape, dtype=np.complex128)
+    r.real = re_
+    r.imag = im
+    return r[()] if r.ndim == 0 else r
+
+
+def mul(a, b):
+    """Multiplication; with a complex operand as compiled code forms it
+    without fused multiply-adds: (ar·br − ai·bi) + (ar·bi + ai·br)i, and
+    component-wise when one operand is real."""
+    if not (np.iscomplexobj(a) or np.iscomplexobj(b)):
+        return a * b
+    ar, ai, ca = _parts(a)
+    br, bi, cb = _parts(b)
+    if ca and cb:
+        return _mkc(ar * br - ai * bi, ar * bi + ai * br)
+    if ca:
+        return _mkc(ar * br, ai * br)
+    return _mkc(ar * br, ar * bi)
+
+
+def _cdiv(a, b):
+    """Complex division as GCC expands it for Fortran (Smith's method with the
+    quotient formed by division), component-wise for a real divisor."""
+    ar, ai, ca = _parts(a)
+    br, bi, cb = _parts(b)
+    if not cb:
+        return _mkc(ar / br, ai / br)
+    if ai is None:
+        ai = np.zeros_like(ar)
+    small = np.abs(br) < np.abs(bi)
+    with np.errstate(all="ignore"):
+        ratio_t = br / bi
+        div_t = br * ratio_t + bi
+        tr_t = (ar * ratio_t + ai) / div_t
+        ti_t = (ai * ratio_t - ar) / div_t
+        ratio_f = bi / br
+        div_f = bi * ratio_f + br
+        tr_f = (ai * ratio_f + ar) / div_f
+        ti_f = (ai - ar * ratio_f) / div_f
+    return _mkc(np.where(small, tr_t, tr_f), np.where(small, ti_t, ti_f))
+
+
 def div(a, b):
+    if np.iscomplexobj(a) or np.iscomplexobj(b):
+        return _cdiv(a, b)
     if _is_int(a) and _is_int(b):
         t = np.result_type(a, b)
         a = np.asarray(a).astype(np.int64)
@@ -350,7 +410,15 @@ INTRINSICS = {
     "btest": "f_btest", "ibset": "f_ibset", "ibclr": "f_ibclr", "ibits": "f_ibits",
     "dble": "R8", "dfloat": "R8", "float": "R4", "real": "_real", "atan": "_atan", "datan": "_atan",
     "log": "_log", "dlog": "_log", "allocated": "_allocated", "present": "_present",
+    "cmplx": "_cmplx", "dcmplx": "_cmplx", "conjg": "np.conj", "dconjg": "np.conj", "aimag": "np.imag",
+    "dimag": "np.imag",
 }
+
+
+def _cmplx(re_, im=0.0, kind=None):
+    if kind is None or int(kind) != 8:
+        return np.complex64(complex(R4(re_), R4(im)))
+    return C16(complex(float(re_), float(im)))
 
 
 def _real(x, kind=None):
@@ -653,6 +721,7 @@ _TYPES = [
     (r"real\s*\(\s*(?:kind\s*=\s*)?8\s*\)|real\*8|double\s+precision", "R8"),
     (r"real\s*\(\s*(?:kind\s*=\s*)?4\s*\)|real\*4|real", "R4"),
     (r"logical\s*\(\s*\d+\s*\)|logical", "LG"),
+    (r"complex\s*\(\s*(?:kind\s*=\s*)?8\s*\)|complex\*16|double\s+complex", "C16"),
 ]
 
 
@@ -703,13 +772,15 @@ class Var:
 class Translator:
     def __init__(self, units, atan, log):
         self.units = units
-        self.ns = {"np": np, "I1": I1, "I4": I4, "I8": I8, "R4": R4, "R8": R8, "LG": LG, "Sect": Sect,
+        self.ns = {"np": np, "I1": I1, "I4": I4, "I8": I8, "R4": R4, "R8": R8, "LG": LG, "C16": C16, "Sect": Sect,
                    "FArr": FArr, "ElemRef": ElemRef, "assoc_array": assoc_array, "assoc_scalar": assoc_scalar,
-                   "new_array": new_array, "val": val, "div": div, "pw": pw, "f_mod": f_mod, "f_int": f_int,
+                   "new_array": new_array, "val": val, "div": div, "mul": mul, "pw": pw, "f_mod": f_mod, "f_int": f_int,
                    "f_nint": f_nint, "f_sign": f_sign, "f_min": f_min, "f_max": f_max, "f_btest": f_btest,
                    "f_ibset": f_ibset, "f_ibclr": f_ibclr, "f_ibits": f_ibits, "f_size": f_size,
                    "_real": _real, "_allocated": _allocated, "FortranStop": FortranStop,
-                   "_atan": lambda x: R8(atan(float(x))), "_log": lambda x: R8(log(float(x)))}
+                   "_cmplx": _cmplx,
+                   "_atan": lambda x: (np.arctan(x) if np.iscomplexobj(x) else R8(atan(float(x)))),
+                   "_log": lambda x: (np.log(x) if np.iscomplexobj(x) else R8(log(float(x))))}
         self.done = set()
 
     def procedure(self, name):
@@ -883,7 +954,7 @@ class Translator:
                 return [f"{p}v_{v.name} = assoc_array(a_{v.name}, {t}, None, ({los},))"]
             his = ", ".join(f"({self.expr(parse_expr(hi))}) - ({self.expr(parse_expr(lo))}) + 1"
                             for lo, hi in v.dims)
-            return [f"{p}v_{v.name} = assoc_array(a_{v.name}, {t}, ({his},), ({los},))"]
+            return [f"{p}v_{v.name} = assoc_array(a_{v.name}, {t}, ({his},), ({los},), {v.intent!r})"]
         if v.alloc:
             return [f"{p}v_{v.name} = None"]
         if v.dims is None:
@@ -940,6 +1011,8 @@ class Translator:
             op, l, r = a
             if op == "/":
                 return f"div({self.expr(l)}, {self.expr(r)})"
+            if op == "*":
+                return f"mul({self.expr(l)}, {self.expr(r)})"
             return f"({self.expr(l)} {op} {self.expr(r)})"
         if k == "ctor":
             return f"np.array([{', '.join(self.expr(x) for x in a[0])}])"

@@ -12,14 +12,16 @@ reference computes in Python is then the reference's own arithmetic: the
 mwm contraction with its q = 0 head and wing terms, the energies at k − q
 (core states first), the spline interpolation of the iopfreq 4 branch and the
 reshape/product of the SVD branch.  The three Fortran kernels it calls
-(fnc.f90: all_fr_convolutions, few_fr_convolutions, many_fr_convolutions)
-cannot be built here; they are supplied by the oracle's restatements, so the
-golden values pin the Python around them, not their own arithmetic (that is
-pinned by known answers in tests/test_oracle_selfc.py).  Output:
+(fnc.f90: all_fr_convolutions, few_fr_convolutions, many_fr_convolutions,
+with fr_convolution2) cannot be compiled here; they run from their Fortran
+text through ``f90py`` (beside this script), with the f2py calling
+convention the reference uses (outputs returned, sizes from the shapes), so
+the golden values are the reference's own statements end to end.  Output:
 ``calc_selfc_golden.npz`` beside this script.
 """
 import io
 import itertools
+import math
 import os
 import sys
 import timeit
@@ -30,9 +32,8 @@ import scipy.interpolate
 import scipy.linalg
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
-from oracle import selfc as osc  # noqa: E402
 sys.path.insert(0, HERE)
+import f90py  # noqa: E402
 import refsrc  # noqa: E402
 from refsrc import NS  # noqa: E402
 
@@ -42,23 +43,49 @@ OUT = os.path.join(HERE, "calc_selfc_golden.npz")
 
 
 def _fnc(enks):
-    """The Fortran kernels as the oracle restates them; each records the
-    energies the reference handed it (once per k-point)."""
+    """The reference's Fortran kernels (fnc.f90), run from their source text,
+    behind the f2py calling convention; each records the energies the
+    reference handed it (once per k-point)."""
+    procs, _ = f90py.load([refsrc.reference_file("fnc.f90")],
+                          ["all_fr_convolutions", "few_fr_convolutions", "many_fr_convolutions"], math.atan, math.log)
+    FA = f90py.FArr
+
     def seen(enk):
         if not enks or not np.array_equal(enks[-1], enk):
             enks.append(np.array(enk))
 
+    def farr(a, dtype):
+        a = np.asfortranarray(np.asarray(a, dtype=dtype))
+        return FA(a, (1,) * a.ndim)
+
+    def i4(x):
+        return np.array(x, dtype=np.int32)
+
     def all_fr_convolutions(enk, mwm, omega, womeg):
         seen(enk)
-        return osc.all_fr_convolutions(enk, mwm, omega, womeg)
+        nom, nb1, nb2 = np.shape(mwm)
+        sc = FA(np.zeros((nb1, nom), dtype=np.complex128, order="F"), (1, 1))
+        procs["all_fr_convolutions"](sc, farr(enk, np.float64), farr(mwm, np.complex128), farr(omega, np.float64),
+                                     farr(womeg, np.float64), i4(nb1), i4(nb2), i4(nom))
+        return sc.a
 
     def few_fr_convolutions(enk, mwmp, mwm_iom, omega, omega_iom, womeg):
         seen(enk)
-        return sum(osc.fr_convolution2(enk[i], mwmp[i, :], mwm_iom[i], omega, omega_iom, womeg) for i in range(len(enk)))
+        nb2, nom = np.shape(mwmp)
+        res = np.zeros((), dtype=np.complex128)
+        procs["few_fr_convolutions"](res, farr(enk, np.float64), farr(mwmp, np.complex128),
+                                     farr(mwm_iom, np.complex128), farr(omega, np.float64),
+                                     np.array(float(omega_iom)), farr(womeg, np.float64), i4(nom), i4(nb2))
+        return res[()]
 
     def many_fr_convolutions(enk, Ul, omega, womeg):
         seen(enk)
-        return osc.many_fr_convolutions(enk, Ul, omega, womeg)
+        nl, nom = np.shape(Ul)
+        nb2 = len(enk)
+        sc = FA(np.zeros((nl, nb2, nom), dtype=np.complex128, order="F"), (1, 1, 1))
+        procs["many_fr_convolutions"](sc, farr(enk, np.float64), farr(Ul, np.complex128), farr(omega, np.float64),
+                                      farr(womeg, np.float64), i4(nom), i4(nl), i4(nb2))
+        return sc.a
     return NS(all_fr_convolutions=all_fr_convolutions, few_fr_convolutions=few_fr_convolutions,
               many_fr_convolutions=many_fr_convolutions)
 

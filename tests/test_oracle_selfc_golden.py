@@ -5,9 +5,10 @@ tests/golden/make_calc_selfc_golden.py:
 
 * mwm for a finite q and for q = 0 with the head and wing terms;
 * the energies at k − q, core states first, against the product's helper;
-* the iopfreq 4 branch (spline interpolation onto the dense mesh) and the SVD
-  branch, whose Fortran convolution kernels the generator supplies from the
-  oracle — so these pin the reference's Python around the kernels.
+* the convolutions of the plain, the iopfreq 4 (spline interpolation onto the
+  dense mesh) and the SVD branches, with the reference's Fortran kernels
+  (fnc.f90) run from their source text by the generator (tests/golden/f90py.py)
+  — the golden values are the reference's own statements end to end.
 """
 import os
 
