@@ -397,6 +397,20 @@ def f_ibits(i, pos, ln):
     return np.array((int(i) >> int(pos)) & ((1 << int(ln)) - 1)).astype(t)[()]
 
 
+def f_matmul(a, b):
+    """matmul of two rank-2 arrays, each element summed over k in ascending
+    order from zero with separate multiplications and additions (the plain
+    loop nest)."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    if a.ndim != 2 or b.ndim != 2 or a.shape[1] != b.shape[0]:
+        raise Unsupported(f"matmul of shapes {a.shape} and {b.shape}")
+    out = np.zeros((a.shape[0], b.shape[1]), dtype=np.result_type(a, b), order="F")
+    for k in range(a.shape[1]):
+        out = out + mul(a[:, k:k + 1], b[k:k + 1, :])
+    return out
+
+
 def f_size(a, dim=None):
     a = val(a)
     return I4(a.size if dim is None else a.shape[int(dim) - 1])
@@ -406,7 +420,7 @@ INTRINSICS = {
     "abs": "np.abs", "dabs": "np.abs", "iabs": "np.abs", "sqrt": "np.sqrt", "dsqrt": "np.sqrt",
     "mod": "f_mod", "int": "f_int", "nint": "f_nint", "sign": "f_sign", "dsign": "f_sign", "isign": "f_sign",
     "min": "f_min", "max": "f_max", "dmin1": "f_min", "dmax1": "f_max", "min0": "f_min", "max0": "f_max",
-    "maxval": "np.max", "minval": "np.min", "sum": "np.sum", "size": "f_size",
+    "maxval": "np.max", "minval": "np.min", "sum": "np.sum", "size": "f_size", "matmul": "f_matmul",
     "btest": "f_btest", "ibset": "f_ibset", "ibclr": "f_ibclr", "ibits": "f_ibits",
     "dble": "R8", "dfloat": "R8", "float": "R4", "real": "_real", "atan": "_atan", "datan": "_atan",
     "log": "_log", "dlog": "_log", "allocated": "_allocated", "present": "_present",
@@ -777,6 +791,7 @@ class Translator:
                    "new_array": new_array, "val": val, "div": div, "mul": mul, "pw": pw, "f_mod": f_mod, "f_int": f_int,
                    "f_nint": f_nint, "f_sign": f_sign, "f_min": f_min, "f_max": f_max, "f_btest": f_btest,
                    "f_ibset": f_ibset, "f_ibclr": f_ibclr, "f_ibits": f_ibits, "f_size": f_size,
+                   "f_matmul": f_matmul,
                    "_real": _real, "_allocated": _allocated, "FortranStop": FortranStop,
                    "_cmplx": _cmplx,
                    "_atan": lambda x: (np.arctan(x) if np.iscomplexobj(x) else R8(atan(float(x)))),

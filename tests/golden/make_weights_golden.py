@@ -17,11 +17,16 @@ arc tangent and logarithm: each case is run twice, once with the C library's
 implementations the oracle and the GPU kernels share, so that the oracle's
 restatement can be compared bit for bit with the reference's statements.
 
+The same is done for ``bz_calcqdepw_par3`` (for_tetrahedra.f90:466-542), the
+weights projected on an SVD frequency basis ``dUl`` (seeded, three
+functions), with ``matmul`` summed over the frequencies in ascending order.
+
 Cases (seeded synthetic band structures with the workload generator's
 shapes): C1-like bands on a 2³ k-mesh, and a stress case whose partially
-occupied bands give polyhedra with 5 to 8 nodes; four imaginary frequencies
-each.  Output: ``weights_golden.npz`` (inputs and the reference's ``kcw`` for
-each math variant); nothing of the reference's source is stored.
+occupied bands give polyhedra with 4, 6 and 8 nodes; four imaginary
+frequencies each.  Output: ``weights_golden.npz`` (inputs and the reference's
+``kcw`` of par2 and par3 for each math variant); nothing of the reference's
+source is stored.
 """
 import math
 import os
@@ -61,6 +66,28 @@ def reference_par2(math_impl):
     return run
 
 
+def reference_par3(math_impl):
+    atan, log = math_impl
+    procs, _ = f90py.load([reference_file(f) for f in FILES], ["bz_calcqdepw_par3"], atan, log)
+    fn = procs["bz_calcqdepw_par3"]
+
+    def run(enk, ef, kqid, ncg, nomx, numin, dUl, omega, tetc):
+        enk = np.asfortranarray(enk, dtype=np.float64)
+        tetc = np.asfortranarray(tetc, dtype=np.int32)
+        nbnd, nkp = enk.shape
+        ntet = tetc.shape[1]
+        nom, nl = dUl.shape
+        nb1, nb2 = ncg + nomx + 1, nbnd - ncg - numin
+        kcw = f90py.FArr(np.zeros((nb1, nb2, nkp, nl), order="F"), (1, 1, 1, 1))
+        i4 = lambda x: np.array(x, dtype=np.int32)     # noqa: E731
+        fn(kcw, f90py.FArr(enk, (1, 1)), np.array(float(ef)), f90py.FArr(np.asarray(kqid, dtype=np.int32).copy(), (1,)),
+           i4(ncg), i4(nomx), i4(numin), f90py.FArr(np.asfortranarray(dUl, dtype=np.float64), (1, 1)),
+           f90py.FArr(np.asarray(omega, dtype=np.float64).copy(), (1,)), f90py.FArr(tetc, (1, 1)), i4(nkp), i4(nom),
+           i4(nbnd), i4(ntet), i4(nl))
+        return kcw.a.copy()
+    return run
+
+
 def cases():
     from pygw_gb300 import synthetic as syn
     out = {}
@@ -95,7 +122,10 @@ def main():
 
     variants = {"libm": (math.atan, math.log), "portable": (portable_atan, portable_log)}
     store = {}
+    rng = np.random.default_rng(2)
     for name, c in cases().items():
+        # an SVD frequency basis for bz_calcqdepw_par3: dUl[nom, nl]
+        c["dUl"] = rng.standard_normal((len(c["omega"]), 3))
         for k, v in c.items():
             store[f"{name}.{k}"] = np.asarray(v)
         for vname, impl in variants.items():
@@ -103,6 +133,11 @@ def main():
             kcw = run(c["enk"], c["ef"], c["kqid"], c["ncg"], c["nomx"], c["numin"], c["omega"], c["tetc"])
             store[f"{name}.kcw_{vname}"] = kcw
             print(f"{name} ({vname}): kcw {kcw.shape}, {np.count_nonzero(kcw)} nonzero", flush=True)
+            run3 = reference_par3(impl)
+            kcw3 = run3(c["enk"], c["ef"], c["kqid"], c["ncg"], c["nomx"], c["numin"], c["dUl"], c["omega"],
+                        c["tetc"])
+            store[f"{name}.kcw3_{vname}"] = kcw3
+            print(f"{name} ({vname}): par3 kcw {kcw3.shape}", flush=True)
     np.savez_compressed(OUT, **store)
     print("wrote", OUT)
 

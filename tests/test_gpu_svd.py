@@ -66,3 +66,21 @@ def test_svd_calc_eps_matches_oracle(precision, tol):
         if iq == 0:
             for a, e in zip(got[1:], ref[1:4]):
                 assert np.max(np.abs(a - e)) <= tol * max(1.0, np.max(np.abs(e)))
+
+
+@pytest.mark.parametrize("name", ["c1", "stress"])
+def test_par3_against_the_reference_statements(name):
+    """The GPU par3 weights against kcw from the reference's own Fortran
+    statements (tests/golden/weights_golden.npz, portable atan/log), within
+    the GPU-vs-oracle par3 bar, outside the entries of 7- and 8-node items
+    (the reference's wtemp layout aliases their frequencies, which the
+    projection mixes into every basis function; see
+    tests/test_oracle_weights_golden.py)."""
+    from test_oracle_weights_golden import alias_mask, item_nodes, load_case
+    a, ref = load_case(name, par=3)
+    got = svd.bz_calcqdepw_par3(a["enk"], a["ef"], a["kqid"], a["ncg"], a["nomx"], a["numin"], a["dUl"], a["omega"],
+                                a["tetc"])
+    want = ref["portable"]
+    assert got.shape == want.shape
+    keep = ~alias_mask(a, item_nodes(a), par=3)
+    assert np.max(np.abs(got - want)[keep]) <= 1e-13 * np.max(np.abs(want))

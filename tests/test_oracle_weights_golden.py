@@ -30,15 +30,16 @@ from oracle import weights as ow
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "weights_golden.npz")
 
 
-def load_case(name):
+def load_case(name, par=2):
     g = np.load(GOLDEN)
-    keys = ("enk", "ef", "kqid", "ncg", "nomx", "numin", "omega", "tetc")
+    keys = ("enk", "ef", "kqid", "ncg", "nomx", "numin", "omega", "tetc", "dUl")
     args = {k: g[f"{name}.{k}"] for k in keys}
     for k in ("ef",):
         args[k] = float(args[k])
     for k in ("ncg", "nomx", "numin"):
         args[k] = int(args[k])
-    return args, {v: g[f"{name}.kcw_{v}"] for v in ("libm", "portable")}
+    tag = "kcw" if par == 2 else "kcw3"
+    return args, {v: g[f"{name}.{tag}_{v}"] for v in ("libm", "portable")}
 
 
 def item_nodes(a):
@@ -65,17 +66,19 @@ def item_nodes(a):
     return out
 
 
-def alias_mask(a, nodes):
+def alias_mask(a, nodes, par=2):
     """kcw entries [ib, jb, k, ω] that 7- and 8-node items touch at the
-    third frequency and later."""
+    third frequency and later (par3: every basis function, the projection
+    mixing all frequencies)."""
     enk, tetc = a["enk"], a["tetc"]
-    nom = len(a["omega"])
+    nw = len(a["omega"]) if par == 2 else a["dUl"].shape[1]
+    first = 2 if par == 2 else 0
     nb1, nb2 = a["ncg"] + a["nomx"] + 1, enk.shape[0] - a["ncg"] - a["numin"]
-    m = np.zeros((nb1, nb2, enk.shape[1], nom), dtype=bool)
+    m = np.zeros((nb1, nb2, enk.shape[1], nw), dtype=bool)
     for (itet, ib, jb), nn in nodes.items():
         if nn >= 7:
             for i in range(4):
-                m[ib, jb, tetc[i, itet], 2:] = True
+                m[ib, jb, tetc[i, itet], first:] = True
     return m
 
 
@@ -96,6 +99,23 @@ def test_oracle_matches_the_reference_statements(name, variant):
         counts = np.bincount(np.array(list(nodes.values())), minlength=9)
         assert all(counts[n] > 0 for n in (4, 6, 8)), counts      # 5 and 7 nodes need degenerate cuts
         assert mask.any() and np.any(diff & mask)        # the aliasing is real, and confined
+
+
+@pytest.mark.parametrize("name", ["c1", "stress"])
+@pytest.mark.parametrize("variant", ["portable", "libm"])
+def test_oracle_par3_matches_the_reference_statements(name, variant):
+    """bz_calcqdepw_par3 (for_tetrahedra.f90:466-542): the weights of all
+    frequencies projected on dUl; bit-identical except the entries of 7- and
+    8-node items, whose aliased frequencies enter every basis function."""
+    a, ref = load_case(name, par=3)
+    got = ow.bz_calcqdepw_par3(a["enk"], a["ef"], a["kqid"], a["ncg"], a["nomx"], a["numin"], a["dUl"], a["omega"],
+                               a["tetc"], libm=(variant == "libm"))
+    want = ref[variant]
+    assert got.shape == want.shape
+    mask = alias_mask(a, item_nodes(a), par=3)
+    diff = got != want
+    assert not np.any(diff & ~mask), np.argwhere(diff & ~mask)[:5]
+    assert np.count_nonzero(want[~mask]) > 0.25 * want.size
 
 
 def test_the_reference_statements_amplify_last_bit_differences_of_atan_log():
