@@ -914,6 +914,13 @@ static int sortnodes(const Nodes& N, int index[9][3], Stats& st) {
 
 // ------------------------------------------------------- convw1t_par
 // for_tetrahedra3.f90:3-136.  weight[i*nom+iom].
+// Reproduce the reference's wtemp layout for 7- and 8-node polyhedra (see
+// convw1t) instead of adding the two halves at every frequency: off by
+// default; the tests switch it on to compare with the reference's statements
+// at every entry.
+static std::atomic<int> g_reference_layout{0};
+extern "C" void oracle_set_reference_layout(int on) { g_reference_layout.store(on ? 1 : 0); }
+
 static void convw1t(double* weight, const double e[4], const double f[4], double ef, const double* omega, int nom,
                     Stats& st) {
   st.calls++;
@@ -977,7 +984,17 @@ static void convw1t(double* weight, const double e[4], const double f[4], double
         if (nnod == 7) genericfunf(dst, tc, e, f, omega, nom, st);
         else genericprism(dst, tc, e, f, omega, nom, st);
       }
-      for (int i = 0; i < 4 * nom; i++) weight[i] = w1[i] + w2[i];
+      if (g_reference_layout.load(std::memory_order_relaxed)) {
+        // the reference's addressing of wtemp(4,2,nom) as (4,nom,2): the first
+        // half's weights survive for the first two frequencies only
+        // (element (c, j) of the Fortran (4, nom) array lies 4·j + c values in;
+        // this restatement stores it at c·nom + j)
+        for (int c = 0; c < 4; c++)
+          for (int j = 0; j < nom; j++)
+            weight[c * nom + j] = (j < 2 ? w1[c * nom + j] : w2[c * nom + j - 2]) + w2[c * nom + j];
+      } else {
+        for (int i = 0; i < 4 * nom; i++) weight[i] = w1[i] + w2[i];
+      }
     } break;
     default:
       st.status |= ERR_NNOD;

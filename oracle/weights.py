@@ -51,6 +51,8 @@ def _lib(libm=False):
         lib.oracle_generictetra.restype = ctypes.c_int
         lib.oracle_portable_math.argtypes = [dp, ctypes.c_int, dp, dp]
         lib.oracle_portable_math.restype = None
+        lib.oracle_set_reference_layout.argtypes = [ctypes.c_int]
+        lib.oracle_set_reference_layout.restype = None
         _LIBS[key] = lib
     return _LIBS[key]
 
@@ -136,3 +138,20 @@ def portable_math(x):
     lg = np.empty_like(x)
     _lib(False).oracle_portable_math(_dp(x), x.shape[0], _dp(a), _dp(lg))
     return a, lg
+
+
+class reference_layout:
+    """Context manager: inside it the restatement reproduces the reference's
+    wtemp(4,2,nom) addressing for 7- and 8-node polyhedra (the first half's
+    weights replaced by the second half's, two frequencies earlier, from the
+    third frequency on) instead of adding the two halves at every frequency."""
+
+    def __enter__(self):
+        for libm in (False, True):
+            _lib(libm).oracle_set_reference_layout(1)
+        return self
+
+    def __exit__(self, *exc):
+        for libm in (False, True):
+            _lib(libm).oracle_set_reference_layout(0)
+        return False

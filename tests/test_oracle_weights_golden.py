@@ -118,6 +118,23 @@ def test_oracle_par3_matches_the_reference_statements(name, variant):
     assert np.count_nonzero(want[~mask]) > 0.25 * want.size
 
 
+@pytest.mark.parametrize("name", ["c1", "stress"])
+@pytest.mark.parametrize("variant", ["portable", "libm"])
+@pytest.mark.parametrize("par", [2, 3])
+def test_oracle_with_the_reference_layout_matches_every_entry(name, variant, par):
+    """With the reference's wtemp addressing reproduced, the restatement
+    equals the reference's statements at every kcw entry, par2 and par3."""
+    a, ref = load_case(name, par=par)
+    with ow.reference_layout():
+        if par == 2:
+            got = ow.bz_calcqdepw_par2(a["enk"], a["ef"], a["kqid"], a["ncg"], a["nomx"], a["numin"], a["omega"],
+                                       a["tetc"], libm=(variant == "libm"))
+        else:
+            got = ow.bz_calcqdepw_par3(a["enk"], a["ef"], a["kqid"], a["ncg"], a["nomx"], a["numin"], a["dUl"],
+                                       a["omega"], a["tetc"], libm=(variant == "libm"))
+    assert np.array_equal(got, ref[variant]), np.abs(got - ref[variant]).max()
+
+
 def test_the_reference_statements_amplify_last_bit_differences_of_atan_log():
     """The reference's own statements with the portable atan/log against the
     C library's: a few-ulp difference in atan/log moves the weights by up to
