@@ -243,6 +243,18 @@ unsigned long long pg_wait_limit_ns(void);
 int pg_set_chi0_prep_batch(int n);
 int pg_chi0_prep_batch(void);
 
+/* How the weights of 7- and 8-node polyhedra (two halves, pentahedra or
+ * prisms) are combined, for every later pg_bz_calcqdepw_par2/par3 call
+ * (process-wide).  0 (default): the two halves' weights are added at every
+ * frequency.  1: the reference's own addressing is reproduced — its
+ * convw1t_par keeps the halves in wtemp(4,2,nom) but addresses that array as
+ * (4,nom,2) (for_tetrahedra3.f90:36, 100-120), so as compiled without bounds
+ * checks the first half's weights are replaced, from the third frequency on,
+ * by the second half's two frequencies earlier; with 1 the results equal the
+ * reference's statements at every entry.  Returns PG_OK. */
+int pg_set_weights_reference_layout(int on);
+int pg_weights_reference_layout(void);
+
 #ifdef __cplusplus
 }
 #endif

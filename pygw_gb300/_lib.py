@@ -63,6 +63,8 @@ SIGNATURES = {
     "pg_wait_limit_ns": (ctypes.c_ulonglong, []),
     "pg_set_chi0_prep_batch": (c_int, [c_int]),
     "pg_chi0_prep_batch": (c_int, []),
+    "pg_set_weights_reference_layout": (c_int, [c_int]),
+    "pg_weights_reference_layout": (c_int, []),
     "pg_eps_inverse_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                                    c_void_p]),
 }

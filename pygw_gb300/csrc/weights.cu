@@ -35,6 +35,7 @@
 // (verified against quadrature); this is kept, since the product must return
 // the reference's results.
 #include <cuda_runtime.h>
+#include <atomic>
 #include <stdint.h>
 #include "fp64_math.h"
 #include "pygw_status.h"
@@ -68,6 +69,7 @@ struct Params {
   double ef;
   int nbnd, nkp, ncg, numin, nb1, nb2, ntet, om0, nomc;
   int tet0;            // first tetrahedron of the chunk
+  int ref_layout;      // reproduce the reference's wtemp addressing (7- and 8-node polyhedra)
 };
 
 struct Ctx {
@@ -1073,7 +1075,7 @@ __global__ void k_class_scatter(const unsigned char* cls, long long nitems, unsi
 // sub-tetrahedra in order (generictetra_par results added one by one), the
 // second polyhedron of a 7- or 8-node item summed separately from 0 and then
 // added (for_tetrahedra3.f90:60-131).
-__global__ void __launch_bounds__(128) k_tet_eval(Params p, long long nitems, const unsigned char* __restrict__ cls) {
+__global__ void __launch_bounds__(128, 4) k_tet_eval(Params p, long long nitems, const unsigned char* __restrict__ cls) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool in = t < nitems * p.nomc;
   Ctx cx;
@@ -1098,34 +1100,56 @@ __global__ void __launch_bounds__(128) k_tet_eval(Params p, long long nitems, co
       const int nsub = nodes_nsub(nnod);
       const SubTet* r = p.recs + p.recoff[li];
       // records in order: the first polyhedron's nsub sub-tetrahedra, then
-      // (7, 8 nodes) the second's; one evaluation site keeps the code small
+      // (7, 8 nodes) the second's; one evaluation site keeps the code small.
+      // With the reference's wtemp addressing (ref_layout) a 7- or 8-node
+      // item's first half is replaced, from the third frequency on, by its
+      // second half two frequencies earlier (for_tetrahedra3.f90:36, 100-120):
+      // the second half's records are evaluated once more at that frequency
+      // (not counted: the reference evaluates each (sub-tetrahedron, ω) once).
       const int nrec = nsub * nodes_ngroup(nnod);
-      double acc[4] = {0.0, 0.0, 0.0, 0.0};
+      const int jg = p.om0 + w;
+      const int nextra = (p.ref_layout && nrec > nsub && jg >= 2) ? nsub : 0;
+      const double omeg_b = nextra ? p.omega[jg - 2] : omeg;
+      double acc[4] = {0.0, 0.0, 0.0, 0.0}, acc_b[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll 1
-      for (int i = 0; i < nrec; i++) {
-        const SubTet& s = r[i];
-        const bool second = i >= nsub;
-        const int st = second ? i - nsub : i;
+      for (int i = 0; i < nrec + nextra; i++) {
+        const bool extra = i >= nrec;
+        const int ri = extra ? i - nsub : i;
+        const SubTet& s = r[ri];
+        const bool second = ri >= nsub;
+        const int st = second ? ri - nsub : ri;
+        const double om_i = extra ? omeg_b : omeg;
         double wo[4] = {0.0, 0.0, 0.0, 0.0};
         const bool live = s.vol >= ZTOL_VOL;
         if (live) {
-          eval_subtet(s, omeg, wo, cx);
-          if (omeg > s.taylor_omega) n_taylor++; else n_exact++;
+          const unsigned long long bw = cx.cnt[PG_CNT_BIGW_WARN], bz = cx.cnt[PG_CNT_BIGW_ZEROED];
+          eval_subtet(s, om_i, wo, cx);
+          if (extra) {
+            cx.cnt[PG_CNT_BIGW_WARN] = bw;
+            cx.cnt[PG_CNT_BIGW_ZEROED] = bz;
+          } else if (om_i > s.taylor_omega) {
+            n_taylor++;
+          } else {
+            n_exact++;
+          }
         }
         if (!second) {
           // the first one sets the slots (0.0 below the volume tolerance),
           // later ones below the tolerance add nothing
 #pragma unroll
           for (int c = 0; c < 4; c++) o[c] = (st == 0) ? wo[c] : (live ? o[c] + wo[c] : o[c]);
-        } else {
+        } else if (!extra) {
           // the second polyhedron sums from 0 on its own, then adds in
 #pragma unroll
           for (int c = 0; c < 4; c++) acc[c] = (st == 0) ? (0.0 + wo[c]) : (acc[c] + wo[c]);
-          if (st == nsub - 1) {
+        } else {
 #pragma unroll
-            for (int c = 0; c < 4; c++) o[c] = o[c] + acc[c];
-          }
+          for (int c = 0; c < 4; c++) acc_b[c] = (st == 0) ? (0.0 + wo[c]) : (acc_b[c] + wo[c]);
         }
+      }
+      if (nrec > nsub) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) o[c] = (nextra ? acc_b[c] : o[c]) + acc[c];
       }
 #pragma unroll
       for (int c = 0; c < 4; c++)
@@ -1300,6 +1324,16 @@ static int enqueue_tet_weights(Params p, const WLayout& L, char* w, cudaStream_t
   return PG_OK;
 }
 
+// Reproduce the reference's addressing of wtemp(4,2,nom) for 7- and 8-node
+// polyhedra (process-wide; read by every later call): off = add the two halves
+// at every frequency.
+static std::atomic<int> g_ref_layout{0};
+extern "C" int pg_set_weights_reference_layout(int on) {
+  g_ref_layout.store(on ? 1 : 0);
+  return PG_OK;
+}
+extern "C" int pg_weights_reference_layout(void) { return g_ref_layout.load(); }
+
 static Params make_params(const double* enk, int nbnd, int nkp, double ef, const int* kqid, int ncg, int numin,
                           int nb1, int nb2, const double* omega, const int* tetc, int ntet, double* scratch,
                           unsigned* d_status, unsigned long long* d_counters) {
@@ -1308,6 +1342,7 @@ static Params make_params(const double* enk, int nbnd, int nkp, double ef, const
   p.enk = enk; p.kqid = kqid; p.omega = omega; p.tetc = tetc; p.scratch = scratch;
   p.status = d_status; p.counters = d_counters; p.ef = ef;
   p.nbnd = nbnd; p.nkp = nkp; p.ncg = ncg; p.numin = numin; p.nb1 = nb1; p.nb2 = nb2; p.ntet = ntet;
+  p.ref_layout = g_ref_layout.load();
   return p;
 }
 

@@ -89,6 +89,24 @@ def weights_device(enk, ef, kqid, ncg, nomx, numin, omega, tetc, nom_chunk=0, st
     return WeightsResult(kcw, status, counters, (nb1, nb2, nkp, nom))
 
 
+class reference_layout:
+    """Context manager: weights computed inside it reproduce the reference's
+    addressing of its wtemp(4,2,nom) array for 7- and 8-node polyhedra
+    (for_tetrahedra3.f90:36, 100-120), equal to the reference's statements at
+    every entry; outside it the two halves are added at every frequency
+    (``pg_set_weights_reference_layout``)."""
+
+    def __enter__(self):
+        lib = _lib.load()
+        self.prev = lib.pg_weights_reference_layout()
+        _lib.check(lib.pg_set_weights_reference_layout(1), "pg_set_weights_reference_layout")
+        return self
+
+    def __exit__(self, *exc):
+        _lib.load().pg_set_weights_reference_layout(self.prev)
+        return False
+
+
 def bz_calcqdepw_par2(enk, ef, kqid, ncg, nomx, numin, omega, tetc):
     """Same call and result as the reference's ``ft.bz_calcqdepw_par2`` (pygw.py:3443)."""
     r = weights_device(enk, ef, kqid, ncg, nomx, numin, omega, tetc)

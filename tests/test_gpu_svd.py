@@ -84,3 +84,17 @@ def test_par3_against_the_reference_statements(name):
     assert got.shape == want.shape
     keep = ~alias_mask(a, item_nodes(a), par=3)
     assert np.max(np.abs(got - want)[keep]) <= 1e-13 * np.max(np.abs(want))
+
+
+@pytest.mark.parametrize("name", ["c1", "stress"])
+def test_par3_reference_layout_against_the_reference_statements(name):
+    """par3 with the reference's wtemp addressing reproduced: within the
+    GPU-vs-oracle par3 bar of the reference's statements at every entry."""
+    from pygw_gb300 import polarization as pol
+    from test_oracle_weights_golden import load_case
+    a, ref = load_case(name, par=3)
+    with pol.reference_layout():
+        got = svd.bz_calcqdepw_par3(a["enk"], a["ef"], a["kqid"], a["ncg"], a["nomx"], a["numin"], a["dUl"],
+                                    a["omega"], a["tetc"])
+    want = ref["portable"]
+    assert np.max(np.abs(got - want)) <= 1e-13 * np.max(np.abs(want))

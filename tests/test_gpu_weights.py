@@ -111,3 +111,25 @@ def test_against_the_reference_statements(name):
     diff = got != want
     mask = alias_mask(a, item_nodes(a))
     assert not np.any(diff & ~mask), np.argwhere(diff & ~mask)[:5]
+
+
+@pytest.mark.parametrize("name", ["c1", "stress"])
+def test_reference_layout_matches_every_entry(name):
+    """With the reference's wtemp addressing reproduced
+    (pg_set_weights_reference_layout), the GPU weights equal the reference's
+    statements at every kcw entry, the frequency-chunked evaluation included."""
+    from test_oracle_weights_golden import load_case
+    a, ref = load_case(name)
+    with pol.reference_layout():
+        for chunk in (0, 1):
+            r = pol.weights_device(a["enk"], a["ef"], a["kqid"], a["ncg"], a["nomx"], a["numin"], a["omega"],
+                                   a["tetc"], nom_chunk=chunk)
+            torch.cuda.synchronize()
+            assert r.status == 0
+            got = r.numpy()
+            assert np.array_equal(got, ref["portable"]), (chunk, np.abs(got - ref["portable"]).max())
+    # and back to the default afterwards
+    r = pol.weights_device(a["enk"], a["ef"], a["kqid"], a["ncg"], a["nomx"], a["numin"], a["omega"], a["tetc"])
+    torch.cuda.synchronize()
+    assert np.array_equal(r.numpy(), ow.bz_calcqdepw_par2(a["enk"], a["ef"], a["kqid"], a["ncg"], a["nomx"],
+                                                         a["numin"], a["omega"], a["tetc"]))
