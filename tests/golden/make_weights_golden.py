@@ -22,9 +22,10 @@ weights projected on an SVD frequency basis ``dUl`` (seeded, three
 functions), with ``matmul`` summed over the frequencies in ascending order.
 
 Cases (seeded synthetic band structures with the workload generator's
-shapes): C1-like bands on a 2³ k-mesh, and a stress case whose partially
-occupied bands give polyhedra with 4, 6 and 8 nodes; four imaginary
-frequencies each.  Output: ``weights_golden.npz`` (inputs and the reference's
+shapes): C1-like bands on a 2³ k-mesh, a stress case whose partially
+occupied bands give polyhedra with 4, 6 and 8 nodes, and a degenerate case
+(energies on a grid of 0.25: values at EF, equal corners) with 5- and 7-node
+polyhedra too; four imaginary frequencies each.  Output: ``weights_golden.npz`` (inputs and the reference's
 ``kcw`` of par2 and par3 for each math variant); nothing of the reference's
 source is stored.
 """
@@ -108,6 +109,14 @@ def cases():
     enk = np.concatenate([np.sort(occ, axis=0), np.sort(emp, axis=0)])
     out["stress"] = dict(enk=np.asfortranarray(enk), ef=0.0, kqid=p.kqm.kqid[:, iq], ncg=0, nomx=2, numin=0,
                          omega=np.array([0.02, 0.2, 2.0, 20.0]), tetc=p.kqm.tetc)
+    # degenerate: the same bands on a grid of 0.25 (energies at EF and equal
+    # corner values), whose polyhedra include 5- and 7-node ones
+    rng = np.random.default_rng(156)
+    occ = np.round(rng.uniform(-0.6, 0.4, (3, nkp)) * 4) / 4
+    emp = np.round(rng.uniform(-0.3, 0.9, (5, nkp)) * 4) / 4
+    enk = np.concatenate([np.sort(occ, axis=0), np.sort(emp, axis=0)])
+    out["degenerate"] = dict(enk=np.asfortranarray(enk), ef=0.0, kqid=p.kqm.kqid[:, iq], ncg=0, nomx=2, numin=0,
+                             omega=np.array([0.02, 0.2, 2.0, 20.0]), tetc=p.kqm.tetc)
     return out
 
 
