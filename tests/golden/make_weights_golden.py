@@ -27,7 +27,9 @@ occupied bands give polyhedra with 4, 6 and 8 nodes, and a degenerate case
 (energies on a grid of 0.25: values at EF, equal corners) with 5- and 7-node
 polyhedra too; four imaginary frequencies each.  Output: ``weights_golden.npz`` (inputs and the reference's
 ``kcw`` of par2 and par3 for each math variant); nothing of the reference's
-source is stored.
+source is stored.  ``--check-c1`` instead compares the oracle (with the
+reference's layout of 7- and 8-node halves) with the reference's statements
+on the full C1 problem and stores nothing.
 """
 import math
 import os
@@ -120,8 +122,32 @@ def cases():
     return out
 
 
+def check_full_c1():
+    """Optional (--check-c1, nothing stored, about ten minutes): the full C1
+    problem (3³ k, 16 × 28 band pairs, four frequencies, the last q) through
+    the reference's statements and through the oracle with the reference's
+    wtemp addressing; prints how many of the kcw entries differ."""
+    from oracle import weights as ow
+    from pygw_gb300 import synthetic as syn
+    w = syn.scaled(syn.WORKLOADS["C1"], div=3, nom=4)
+    p = syn.Problem(w)
+    b = p.bands
+    nomx, numin = b.nomax_numin
+    args = (b.enk(), b.EF, p.kqm.kqid[:, p.qs[-1]], 0, nomx, numin, p.fr.omega, p.kqm.tetc)
+    portable = (lambda x: float(ow.portable_math(np.array([x]))[0][0]),
+                lambda x: float(ow.portable_math(np.array([x]))[1][0]))
+    ref = reference_par2(portable)(*args)
+    with ow.reference_layout():
+        got = ow.bz_calcqdepw_par2(*args)
+    print(f"full C1: kcw {ref.shape}, {np.count_nonzero(ref)} nonzero, "
+          f"{np.count_nonzero(got != ref)} entries differ from the reference's statements")
+
+
 def main():
     from oracle import weights as ow
+    if "--check-c1" in sys.argv:
+        check_full_c1()
+        return
 
     def portable_atan(x):
         return float(ow.portable_math(np.array([x]))[0][0])
