@@ -180,7 +180,6 @@ def assoc_array(actual, dtype, dims, lbs, intent=None):
     actual) with lower bounds ``lbs``, associated with ``actual``."""
     if isinstance(actual, ElemRef):
         src = actual.arr.a
-        start = src[actual.ni]
         first = src[tuple(slice(i, i + 1) for i in actual.ni)]
     elif isinstance(actual, FArr):
         src = actual.a
@@ -423,7 +422,7 @@ INTRINSICS = {
     "maxval": "np.max", "minval": "np.min", "sum": "np.sum", "size": "f_size", "matmul": "f_matmul",
     "btest": "f_btest", "ibset": "f_ibset", "ibclr": "f_ibclr", "ibits": "f_ibits",
     "dble": "R8", "dfloat": "R8", "float": "R4", "real": "_real", "atan": "_atan", "datan": "_atan",
-    "log": "_log", "dlog": "_log", "allocated": "_allocated", "present": "_present",
+    "log": "_log", "dlog": "_log", "allocated": "_allocated",
     "cmplx": "_cmplx", "dcmplx": "_cmplx", "conjg": "np.conj", "dconjg": "np.conj", "aimag": "np.imag",
     "dimag": "np.imag",
 }
@@ -1055,7 +1054,7 @@ class Translator:
                 for x in args:
                     if x.kind == "kw":
                         vals.append(self.expr(x.args[1]))
-                    elif nm in ("allocated", "present", "size"):
+                    elif nm in ("allocated", "size"):
                         vals.append(self.expr(x, ctx="arg"))
                     else:
                         vals.append(self.expr(x))
