@@ -25,7 +25,9 @@ Cases (seeded synthetic band structures with the workload generator's
 shapes): C1-like bands on a 2³ k-mesh, a stress case whose partially
 occupied bands give polyhedra with 4, 6 and 8 nodes, and a degenerate case
 (energies on a grid of 0.25: values at EF, equal corners) with 5- and 7-node
-polyhedra too; four imaginary frequencies each.  Output: ``weights_golden.npz`` (inputs and the reference's
+polyhedra too; four imaginary frequencies each; and a case with a core
+state and an offset empty-band window (ncg = 1, numin = 1), three
+frequencies.  Output: ``weights_golden.npz`` (inputs and the reference's
 ``kcw`` of par2 and par3 for each math variant); nothing of the reference's
 source is stored.  ``--check-c1`` instead compares the oracle (with the
 reference's layout of 7- and 8-node halves) with the reference's statements
@@ -119,6 +121,15 @@ def cases():
     enk = np.concatenate([np.sort(occ, axis=0), np.sort(emp, axis=0)])
     out["degenerate"] = dict(enk=np.asfortranarray(enk), ef=0.0, kqid=p.kqm.kqid[:, iq], ncg=0, nomx=2, numin=0,
                              omega=np.array([0.02, 0.2, 2.0, 20.0]), tetc=p.kqm.tetc)
+    # band-window offsets: one core state below the bands (ncg = 1) and the
+    # lowest band left out of the empty window (numin = 1)
+    rng = np.random.default_rng(21)
+    core = np.full((1, nkp), -5.0)
+    occ = rng.uniform(-0.6, 0.4, (3, nkp))
+    emp = rng.uniform(-0.3, 0.9, (4, nkp))
+    enk = np.concatenate([core, np.sort(occ, axis=0), np.sort(emp, axis=0)])
+    out["offsets"] = dict(enk=np.asfortranarray(enk), ef=0.0, kqid=p.kqm.kqid[:, iq], ncg=1, nomx=2, numin=1,
+                          omega=np.array([0.05, 0.5, 5.0]), tetc=p.kqm.tetc)
     return out
 
 

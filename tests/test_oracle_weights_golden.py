@@ -82,7 +82,7 @@ def alias_mask(a, nodes, par=2):
     return m
 
 
-@pytest.mark.parametrize("name", ["c1", "stress", "degenerate"])
+@pytest.mark.parametrize("name", ["c1", "stress", "degenerate", "offsets"])
 @pytest.mark.parametrize("variant", ["portable", "libm"])
 def test_oracle_matches_the_reference_statements(name, variant):
     a, ref = load_case(name)
@@ -103,7 +103,7 @@ def test_oracle_matches_the_reference_statements(name, variant):
         assert all(counts[n] > 0 for n in (4, 5, 6, 7, 8)), counts
 
 
-@pytest.mark.parametrize("name", ["c1", "stress", "degenerate"])
+@pytest.mark.parametrize("name", ["c1", "stress", "degenerate", "offsets"])
 @pytest.mark.parametrize("variant", ["portable", "libm"])
 def test_oracle_par3_matches_the_reference_statements(name, variant):
     """bz_calcqdepw_par3 (for_tetrahedra.f90:466-542): the weights of all
@@ -120,7 +120,7 @@ def test_oracle_par3_matches_the_reference_statements(name, variant):
     assert np.count_nonzero(want[~mask]) > 0.25 * want.size
 
 
-@pytest.mark.parametrize("name", ["c1", "stress", "degenerate"])
+@pytest.mark.parametrize("name", ["c1", "stress", "degenerate", "offsets"])
 @pytest.mark.parametrize("variant", ["portable", "libm"])
 @pytest.mark.parametrize("par", [2, 3])
 def test_oracle_with_the_reference_layout_matches_every_entry(name, variant, par):
