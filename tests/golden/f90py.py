@@ -25,8 +25,13 @@ Only the constructs these routines use are supported; anything else raises
 ``Unsupported`` at translation time.  Intrinsic functions map to numpy, except
 that ``atan`` and ``log`` (and their D-prefixed forms) call functions the
 caller supplies, so a comparison can use the same implementations on both
-sides.  Nothing of the reference's source is stored: the text is read from
-the reference tree each time.
+sides.  Local variables and allocated arrays start at zero; with ``POISON``
+set, their real and complex elements start at NaN and their integers at the
+type's lowest value instead, and a bit test at a position outside the
+integer raises ``Undefined``, so a result that depends on storage never
+written (which compiled code leaves uninitialised) comes out NaN or raises.
+Nothing of the reference's source is stored: the text is read from the
+reference tree each time.
 """
 from __future__ import annotations
 
@@ -41,6 +46,12 @@ class Unsupported(Exception):
 
 class FortranStop(Exception):
     pass
+
+
+class Undefined(IndexError):
+    """The statements do something whose result compiled code leaves
+    undefined: address outside an array's storage, or test a bit at a
+    position outside the integer."""
 
 
 # ----------------------------------------------------------------- runtime
@@ -129,7 +140,7 @@ class FArr:
         lo_b = off + sum(min(0, (c - 1) * s) for c, s in zip(counts, strides) if c > 0)
         hi_b = off + sum(max(0, (c - 1) * s) for c, s in zip(counts, strides) if c > 0)
         if lo_b < 0 or hi_b + self.a.itemsize > base.nbytes:
-            raise IndexError("subscript outside the array's storage")
+            raise Undefined("subscript outside the array's storage")
         v = np.ndarray(tuple(counts), dtype=self.a.dtype, buffer=base, offset=off, strides=tuple(strides))
         return v[tuple(slice(None) if k else 0 for k in keep)]
 
@@ -235,10 +246,31 @@ def assoc_scalar(actual, dtype):
     return np.array(actual, dtype=dtype)
 
 
+# local variables and allocated arrays start at zero, or (POISON) at a value
+# that shows a read before the first write
+POISON = False
+
+
+def _unset(dtype):
+    dt = np.dtype(dtype)
+    if POISON and np.issubdtype(dt, np.inexact):
+        return np.nan
+    if POISON and np.issubdtype(dt, np.integer):
+        return np.iinfo(dt).min
+    return 0
+
+
+def unset_scalar(dtype):
+    return np.array(_unset(dtype), dtype=dtype)
+
+
 def new_array(dtype, bounds):
     lbs = [lo for lo, hi in bounds]
     shape = [max(0, int(hi) - int(lo) + 1) for lo, hi in bounds]
-    return FArr(np.zeros(shape, dtype=dtype, order="F"), lbs)
+    a = np.zeros(shape, dtype=dtype, order="F")
+    if _unset(dtype) != 0:
+        a.fill(_unset(dtype))
+    return FArr(a, lbs)
 
 
 def val(x):
@@ -377,23 +409,29 @@ def f_max(*xs):
     return np.asarray(r, dtype=t)[()]
 
 
+def _bitpos(i, pos):
+    if not 0 <= int(pos) < 8 * np.asarray(i).dtype.itemsize:
+        raise Undefined(f"bit position {int(pos)}")
+    return int(pos)
+
+
 def f_btest(i, pos):
-    return bool((int(i) >> int(pos)) & 1)
+    return bool((int(i) >> _bitpos(i, pos)) & 1)
 
 
 def f_ibset(i, pos):
     t = np.asarray(i).dtype
-    return np.array(int(i) | (1 << int(pos))).astype(t)[()]
+    return np.array(int(i) | (1 << _bitpos(i, pos))).astype(t)[()]
 
 
 def f_ibclr(i, pos):
     t = np.asarray(i).dtype
-    return np.array(int(i) & ~(1 << int(pos))).astype(t)[()]
+    return np.array(int(i) & ~(1 << _bitpos(i, pos))).astype(t)[()]
 
 
 def f_ibits(i, pos, ln):
     t = np.asarray(i).dtype
-    return np.array((int(i) >> int(pos)) & ((1 << int(ln)) - 1)).astype(t)[()]
+    return np.array((int(i) >> _bitpos(i, pos)) & ((1 << int(ln)) - 1)).astype(t)[()]
 
 
 def f_matmul(a, b):
@@ -787,7 +825,8 @@ class Translator:
         self.units = units
         self.ns = {"np": np, "I1": I1, "I4": I4, "I8": I8, "R4": R4, "R8": R8, "LG": LG, "C16": C16, "Sect": Sect,
                    "FArr": FArr, "ElemRef": ElemRef, "assoc_array": assoc_array, "assoc_scalar": assoc_scalar,
-                   "new_array": new_array, "val": val, "div": div, "mul": mul, "pw": pw, "f_mod": f_mod, "f_int": f_int,
+                   "new_array": new_array, "unset_scalar": unset_scalar, "val": val, "div": div, "mul": mul,
+                   "pw": pw, "f_mod": f_mod, "f_int": f_int,
                    "f_nint": f_nint, "f_sign": f_sign, "f_min": f_min, "f_max": f_max, "f_btest": f_btest,
                    "f_ibset": f_ibset, "f_ibclr": f_ibclr, "f_ibits": f_ibits, "f_size": f_size,
                    "f_matmul": f_matmul,
@@ -796,6 +835,7 @@ class Translator:
                    "_atan": lambda x: (np.arctan(x) if np.iscomplexobj(x) else R8(atan(float(x)))),
                    "_log": lambda x: (np.log(x) if np.iscomplexobj(x) else R8(log(float(x))))}
         self.done = set()
+        self.sources = {}       # unit name -> generated Python source
 
     def procedure(self, name):
         if name not in self.done:
@@ -807,6 +847,7 @@ class Translator:
         src = self.emit_unit(u, host_vars or {}, indent)
         if indent == 0:
             code = "\n".join(src)
+            self.sources[u.name] = code
             try:
                 exec(compile(code, f"<f90:{u.name}>", "exec"), self.ns)
             except SyntaxError as e:
@@ -972,8 +1013,9 @@ class Translator:
         if v.alloc:
             return [f"{p}v_{v.name} = None"]
         if v.dims is None:
-            init = self.expr(parse_expr(v.init)) if v.init else "0"
-            return [f"{p}v_{v.name} = np.array({init}, dtype={t})"]
+            if not v.init:
+                return [f"{p}v_{v.name} = unset_scalar({t})"]
+            return [f"{p}v_{v.name} = np.array({self.expr(parse_expr(v.init))}, dtype={t})"]
         bounds = ", ".join(f"({self.expr(parse_expr(lo))}, {self.expr(parse_expr(hi))})" for lo, hi in v.dims)
         out = [f"{p}v_{v.name} = new_array({t}, [{bounds}])"]
         if v.init:
@@ -1303,6 +1345,52 @@ def _frange(lo, hi, st):
     lo, hi, st = int(lo), int(hi), int(st)
     n = max(0, (hi - lo + st) // st) if st > 0 else max(0, (lo - hi - st) // (-st))
     return [lo + k * st for k in range(n)]
+
+
+class LineTrace:
+    """Context manager recording which lines of the translated procedures
+    run (``hits``: {unit name: set of line numbers of its generated source})."""
+
+    def __init__(self):
+        import collections
+        self.hits = collections.defaultdict(set)
+
+    def _global(self, frame, event, arg):
+        if not frame.f_code.co_filename.startswith("<f90:"):
+            return None
+        return self._local
+
+    def _local(self, frame, event, arg):
+        if event == "line":
+            self.hits[frame.f_code.co_filename[5:-1]].add(frame.f_lineno)
+        return self._local
+
+    def __enter__(self):
+        import sys
+        sys.settrace(self._global)
+        return self
+
+    def __exit__(self, *exc):
+        import sys
+        sys.settrace(None)
+        return False
+
+
+def unexecuted(tr, hits):
+    """{unit name: (executed, executable, [generated lines never run])} for
+    every procedure ``tr`` translated, given ``LineTrace.hits``."""
+    out = {}
+    for name, src in sorted(tr.sources.items()):
+        lines, stack = set(), [compile(src, f"<f90:{name}>", "exec")]
+        while stack:
+            c = stack.pop()
+            lines.update(ln for _, _, ln in c.co_lines() if ln)
+            stack.extend(x for x in c.co_consts if hasattr(x, "co_lines"))
+        text = src.split("\n")
+        lines = {ln for ln in lines if not text[ln - 1].lstrip().startswith("def ")}
+        miss = sorted(lines - hits.get(name, set()))
+        out[name] = (len(lines) - len(miss), len(lines), [text[ln - 1].strip() for ln in miss])
+    return out
 
 
 def load(paths, names, atan, log):

@@ -32,6 +32,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 import f90py  # noqa: E402
+f90py.POISON = True     # a read of storage never written shows as NaN, or raises
 import refsrc  # noqa: E402
 from refsrc import NS  # noqa: E402
 

@@ -25,13 +25,19 @@ Cases (seeded synthetic band structures with the workload generator's
 shapes): C1-like bands on a 2³ k-mesh, a stress case whose partially
 occupied bands give polyhedra with 4, 6 and 8 nodes, and a degenerate case
 (energies on a grid of 0.25: values at EF, equal corners) with 5- and 7-node
-polyhedra too; four imaginary frequencies each; and a case with a core
-state and an offset empty-band window (ncg = 1, numin = 1), three
-frequencies.  Output: ``weights_golden.npz`` (inputs and the reference's
-``kcw`` of par2 and par3 for each math variant); nothing of the reference's
-source is stored.  ``--check-c1`` instead compares the oracle (with the
-reference's layout of 7- and 8-node halves) with the reference's statements
-on the full C1 problem and stores nothing.
+polyhedra too; four imaginary frequencies each; a case with a core state
+and an offset empty-band window (ncg = 1, numin = 1), three frequencies; and
+a static-limit case at q = Γ (frequencies 0 and 1e-7, a band pair 1e-7
+apart, a six-node polyhedron with two quadrilateral faces) that reaches the
+branches the other cases leave unexecuted.  The statements run with
+``f90py.POISON`` on, so a weight that depended on storage never written
+would come out NaN (the script then stops).
+
+Output: ``weights_golden.npz`` (inputs and the reference's ``kcw`` of par2
+and par3 for each math variant); nothing of the reference's source is
+stored.  ``--check-c1`` instead compares the oracle (with the reference's
+layout of 7- and 8-node halves) with the reference's statements on the full
+C1 problem and stores nothing.
 """
 import math
 import os
@@ -44,6 +50,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, HERE)
 sys.path.insert(0, ROOT)
 import f90py  # noqa: E402
+f90py.POISON = True     # a read of storage never written shows as NaN, or raises
 from refsrc import reference_file  # noqa: E402
 
 OUT = os.path.join(HERE, "weights_golden.npz")
@@ -67,6 +74,7 @@ def reference_par2(math_impl):
         fn(kcw, f90py.FArr(enk, (1, 1)), np.array(float(ef)), f90py.FArr(np.asarray(kqid, dtype=np.int32).copy(), (1,)),
            i4(ncg), i4(nomx), i4(numin), f90py.FArr(np.asarray(omega, dtype=np.float64).copy(), (1,)),
            f90py.FArr(tetc, (1, 1)), i4(nkp), i4(nom), i4(nbnd), i4(ntet))
+        assert np.isfinite(kcw.a).all(), "the statements read storage they never wrote"
         return kcw.a.copy()
     return run
 
@@ -89,6 +97,7 @@ def reference_par3(math_impl):
            i4(ncg), i4(nomx), i4(numin), f90py.FArr(np.asfortranarray(dUl, dtype=np.float64), (1, 1)),
            f90py.FArr(np.asarray(omega, dtype=np.float64).copy(), (1,)), f90py.FArr(tetc, (1, 1)), i4(nkp), i4(nom),
            i4(nbnd), i4(ntet), i4(nl))
+        assert np.isfinite(kcw.a).all(), "the statements read storage they never wrote"
         return kcw.a.copy()
     return run
 
@@ -130,6 +139,21 @@ def cases():
     enk = np.concatenate([core, np.sort(occ, axis=0), np.sort(emp, axis=0)])
     out["offsets"] = dict(enk=np.asfortranarray(enk), ef=0.0, kqid=p.kqm.kqid[:, iq], ncg=1, nomx=2, numin=1,
                           omega=np.array([0.05, 0.5, 5.0]), tetc=p.kqm.tetc)
+    # static limit: q = Γ (k - q = k), frequencies 0 and 1e-7 besides finite
+    # ones, a band 1e-7 above the lowest one at half of the k-points (weights
+    # beyond stweight_imag_par's unphysical-weight tolerance, zeroed below
+    # |ω| = 1e-6), and one tetrahedron whose polyhedron has six nodes with
+    # two quadrilateral faces (sortnodes' two-square branch)
+    rng = np.random.default_rng(0)
+    occ = rng.uniform(-0.6, 0.4, (3, nkp))
+    emp = rng.uniform(-0.3, 0.9, (2, nkp))
+    near = occ[:1] + 1e-7 * rng.choice([0.0, 1.0], (1, nkp))
+    enk = np.concatenate([occ, near, emp])
+    c0 = p.kqm.tetc[:, 0]
+    enk[0, c0] = [-1.0, -0.25, 0.5, -0.5]
+    enk[4, c0] = [0.5, 0.0, -0.25, 0.75]
+    out["static"] = dict(enk=np.asfortranarray(enk), ef=0.0, kqid=np.arange(nkp), ncg=0, nomx=2, numin=0,
+                         omega=np.array([0.0, 1e-7, 1e-3, 0.5, 5.0]), tetc=p.kqm.tetc)
     return out
 
 

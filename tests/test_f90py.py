@@ -5,7 +5,9 @@ Each case is a few lines of Fortran whose compiled result is known: kinds and
 mixed-kind arithmetic, integer division and MOD, integer powers, sequence
 association of array arguments (including the out-of-bounds addressing the
 reference's wtemp relies on), statement functions, internal procedures,
-SELECT CASE, DO loops with exits, and complex division as GCC forms it.
+SELECT CASE, DO loops with exits, complex division as GCC forms it, the
+poisoned start values that expose reads of storage never written, and the
+line trace that lists the statements a run never executed.
 """
 import math
 import os
@@ -190,3 +192,53 @@ end subroutine bad
 """
     with pytest.raises(f90py.Unsupported):
         _load(src, ["bad"], tmp_path)
+
+
+def test_poison_shows_reads_of_storage_never_written(tmp_path, monkeypatch):
+    src = """
+subroutine unset(x, n, b)
+  implicit none
+  real(8), intent(out) :: x
+  integer, intent(out) :: n
+  logical, intent(out) :: b
+  real(8) :: w(3)
+  integer :: k(2)
+  w(1) = 1.0d0
+  w(2) = 2.0d0
+  x = w(1) + w(3)
+  k(1) = 5
+  n = k(2)
+  b = btest(5, k(2))
+end subroutine unset
+"""
+    f = _load(src, ["unset"], tmp_path)["unset"]
+    x, n, b = np.array(0.0), i4(0), np.array(False)
+    f(x, n, b)                                   # default: storage starts at zero
+    assert (x[()], n[()], b[()]) == (1.0, 0, True)
+    monkeypatch.setattr(f90py, "POISON", True)
+    with pytest.raises(f90py.Undefined):         # a bit position never set
+        f(x, n, b)
+    assert np.isnan(x[()]) and n[()] == np.iinfo(np.int32).min
+
+
+def test_line_trace_lists_the_statements_never_executed(tmp_path):
+    src = """
+subroutine pick(i, r)
+  implicit none
+  integer, intent(in) :: i
+  integer, intent(out) :: r
+  if (i > 0) then
+     r = 1
+  else
+     r = -1
+  endif
+end subroutine pick
+"""
+    path = tmp_path / "t.f90"
+    path.write_text(src)
+    procs, tr = f90py.load([str(path)], ["pick"], math.atan, math.log)
+    r = i4(0)
+    with f90py.LineTrace() as t:
+        procs["pick"](i4(3), r)
+    ran, total, never = f90py.unexecuted(tr, t.hits)["pick"]
+    assert r[()] == 1 and ran == total - 1 and len(never) == 1 and "-" in never[0]

@@ -1,0 +1,91 @@
+"""The oracle's per-tetrahedron weights against the reference's own statements (CPU).
+
+``tests/golden/tetra_golden.npz`` holds, for 1100 seeded corner-energy sets
+(e occupied, f empty, EF = 0; energies on a grid of 0.25, pairs 0 to 0.25
+apart, continuous values, and f - e equal or nearly equal across the corners), what the reference's ``convw1t_par`` and its
+callees (for_tetrahedra3.f90:3-743, for_tetrahedra2.f90:1688-2773) compute
+when executed from their Fortran text by ``tests/golden/make_tetra_golden.py``,
+at six imaginary frequencies including 0 and 1e-7: the 4 × nom corner weights,
+or the verdict that the statements address outside an array (undefined in
+compiled code) or call ``stop``.  The corner sets cover every polyhedron node
+count and every branch of ``sortnodes`` that orders well-defined polyhedra.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import weights as ow
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "tetra_golden.npz")
+ERR_UNDEFINED = 1 << 5
+ERR_STOP = (1 << 0) | (1 << 1) | (1 << 2) | (1 << 3) | (1 << 4)   # the reference's stop sites
+
+
+@pytest.fixture(scope="module")
+def golden():
+    g = np.load(GOLDEN)
+    return {k: g[k] for k in g.files}
+
+
+def _run(g, i):
+    return ow.convw1t(g["e"][i], g["f"][i], 0.0, g["omega"])
+
+
+def test_well_defined_tetrahedra_match_bit_for_bit(golden):
+    """With the reference's wtemp addressing for 7- and 8-node polyhedra,
+    every weight of every well-defined tetrahedron is bit-identical."""
+    g = golden
+    ok = np.flatnonzero(g["kind"] == 0)
+    assert len(ok) > 800
+    nnods = []
+    with ow.reference_layout():
+        for i in ok:
+            w, st, nn = _run(g, i)
+            assert st == 0, (i, st)
+            assert np.array_equal(w, g["weight"][i]), (i, g["e"][i], g["f"][i], np.abs(w - g["weight"][i]).max())
+            nnods.append(nn)
+    counts = np.bincount(nnods, minlength=9)
+    assert all(counts[n] > 0 for n in range(3, 9)), counts
+
+
+def test_default_layout_differs_only_where_the_halves_alias(golden):
+    """Without the reference's layout the oracle adds the two halves of a
+    7- or 8-node polyhedron at every frequency; it then differs from the
+    statements only at those polyhedra, from the third frequency on."""
+    g = golden
+    aliased = 0
+    for i in np.flatnonzero(g["kind"] == 0):
+        w, st, nn = _run(g, i)
+        d = w != g["weight"][i]
+        if nn < 7:
+            assert not d.any(), i
+        else:
+            assert not d[:, :2].any(), i
+            aliased += bool(d.any())
+    assert aliased > 0
+
+
+def test_undefined_and_stopping_tetrahedra_are_flagged(golden):
+    """Where the statements leave an array's storage the oracle reports
+    PG_ERR_UNDEFINED; where they call stop it reports the stop site's bit."""
+    g = golden
+    k = g["kind"]
+    assert (k == 1).any() and (k == 2).any()
+    for i in np.flatnonzero(k == 1):
+        _, st, _ = _run(g, i)
+        assert st & ERR_UNDEFINED, (i, st)
+    for i in np.flatnonzero(k == 2):
+        _, st, _ = _run(g, i)
+        assert st & (ERR_STOP | ERR_UNDEFINED), (i, st)
+
+
+def test_static_limit_branches_are_present(golden):
+    """The fixture reaches ω = 0 (the arc tangent's limit ±π/2), weights
+    beyond the unphysical tolerance zeroed below |ω| = 1e-6, and finite
+    weights there."""
+    g = golden
+    ok = g["kind"] == 0
+    w = g["weight"][ok]
+    assert g["omega"][0] == 0.0 and np.isfinite(w).all()
+    assert np.count_nonzero(w[:, :, 0]) > 100

@@ -82,7 +82,7 @@ def alias_mask(a, nodes, par=2):
     return m
 
 
-@pytest.mark.parametrize("name", ["c1", "stress", "degenerate", "offsets"])
+@pytest.mark.parametrize("name", ["c1", "stress", "degenerate", "offsets", "static"])
 @pytest.mark.parametrize("variant", ["portable", "libm"])
 def test_oracle_matches_the_reference_statements(name, variant):
     a, ref = load_case(name)
@@ -101,9 +101,16 @@ def test_oracle_matches_the_reference_statements(name, variant):
         assert mask.any() and np.any(diff & mask)        # the aliasing is real, and confined
     if name == "degenerate":
         assert all(counts[n] > 0 for n in (4, 5, 6, 7, 8)), counts
+    if name == "static":
+        # ω = 0 weights are finite and nonzero; some exceeded the unphysical
+        # tolerance below |ω| = 1e-6 and were zeroed (for_tetrahedra3.f90:694-708)
+        _, _, stats = ow.bz_calcqdepw_par2(a["enk"], a["ef"], a["kqid"], a["ncg"], a["nomx"], a["numin"],
+                                           a["omega"], a["tetc"], return_stats=True)
+        assert a["omega"][0] == 0.0 and np.isfinite(want).all() and np.count_nonzero(want[..., 0]) > 0
+        assert stats["big_weight_zeroed"] > 0, stats
 
 
-@pytest.mark.parametrize("name", ["c1", "stress", "degenerate", "offsets"])
+@pytest.mark.parametrize("name", ["c1", "stress", "degenerate", "offsets", "static"])
 @pytest.mark.parametrize("variant", ["portable", "libm"])
 def test_oracle_par3_matches_the_reference_statements(name, variant):
     """bz_calcqdepw_par3 (for_tetrahedra.f90:466-542): the weights of all
@@ -117,10 +124,12 @@ def test_oracle_par3_matches_the_reference_statements(name, variant):
     mask = alias_mask(a, item_nodes(a), par=3)
     diff = got != want
     assert not np.any(diff & ~mask), np.argwhere(diff & ~mask)[:5]
-    assert np.count_nonzero(want[~mask]) > 0.25 * want.size
+    # the static case's polyhedra are mostly 8-node ones, so few entries are
+    # free of the aliasing there (every entry is compared with the layout on)
+    assert np.count_nonzero(want[~mask]) > (0.02 if name == "static" else 0.25) * want.size
 
 
-@pytest.mark.parametrize("name", ["c1", "stress", "degenerate", "offsets"])
+@pytest.mark.parametrize("name", ["c1", "stress", "degenerate", "offsets", "static"])
 @pytest.mark.parametrize("variant", ["portable", "libm"])
 @pytest.mark.parametrize("par", [2, 3])
 def test_oracle_with_the_reference_layout_matches_every_entry(name, variant, par):
