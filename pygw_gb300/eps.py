@@ -411,6 +411,39 @@ def chi0_eps(kcw, minm, nkp, npb, nb1, nb2, nom, pm_k=None, head=None, k_chunk=N
     return out
 
 
+def momentum_vectors(head_quantities, ks, core, kqm, vol, isp=0):
+    """The q→0 vectors ``pm[ik, (ncg_p + nvbm)·nb2]`` that calc_eps forms from
+    the momentum matrix elements in ``head_quantities = (head, mmatcv,
+    mmatvv, mst)`` (pygw.py:3120-3141), core states first: for each
+    (occupied or core, empty) pair the x + y + z sum of ⟨p⟩ (stored from band
+    ``mst`` on) times 2√(π/Vol)/√3, divided by the energy difference, or 0
+    where the two energies are within 1e-10.  The energies are the core
+    levels ``core.eig_core[isp][iat][ic]`` of ``core.corind`` and the bands
+    of the irreducible k point (pygw.py:3089-3093).  Host-side argument
+    assembly: a few thousand entries per k point."""
+    _, mmatcv, mmatvv, mst = head_quantities
+    nvbm, ncbm = ks.nomax_numin[0] + 1, ks.nomax_numin[1]
+    nbmax, ncg = ks.nbmaxpol, ks.ncg_p
+    coefw = 2.0 * np.sqrt(np.pi / vol)
+    scale = coefw / np.sqrt(3.0)
+    corind = np.asarray(core.corind)
+    ecore = np.array([core.eig_core[isp][int(iat)][int(ic)] for iat, _, ic in corind[:ncg, :3]], dtype=np.float64)
+    pm = np.zeros((len(kqm.kii_ind), (ncg + nvbm) * (nbmax - ncbm)), dtype=np.complex128)
+    for ik, irk in enumerate(kqm.kii_ind):
+        eb = np.asarray(ks.Ebnd[isp, irk, :nbmax], dtype=np.float64)
+        mmc = np.sum(mmatcv[irk, ncbm - mst:nbmax - mst, :, :], axis=2) * scale    # [nb2, ncg]
+        mmv = np.sum(mmatvv[irk, ncbm - mst:nbmax - mst, :, :], axis=2) * scale    # [nb2, nvbm]
+        rows = []
+        for e1, m in ((ecore, mmc[:, :ncg]), (eb[:nvbm], mmv[:, :nvbm])):
+            edif = e1[:, None] - eb[None, ncbm:nbmax]
+            big = np.abs(edif) > 1e-10
+            r = np.zeros(edif.shape, dtype=np.complex128)
+            r[big] = m.T[big] / edif[big]
+            rows.append(r)
+        pm[ik] = np.concatenate(rows, axis=0).ravel()
+    return pm
+
+
 class MatrixElements2Band:
     """Stand-in for the reference class with the GB300 ``calc_eps`` and ``calc_selfc``.
 
@@ -419,6 +452,10 @@ class MatrixElements2Band:
     'polarization', 3342-3349 for 'selfe'); the synthetic generator provides
     one (``synthetic_matrix_elements``).  singc1/singc2 are the q→0
     singularity coefficients calc_selfc uses at q = 0 (pygw.py:3310-3311).
+    At q = 0 calc_eps forms the wings' vectors from ``head_quantities`` as
+    the reference does (``momentum_vectors``) unless ``pm_k(ik)`` is given
+    here, which then supplies them directly (the synthetic workloads draw
+    them per k point).
     """
 
     def __init__(self, calc_minm, matsize, pm_k=None, singc1=0.0, singc2=0.0):
@@ -444,6 +481,9 @@ class MatrixElements2Band:
         if iq == 0:
             head = head_quantities[0]
             pm_k = self.pm_k
+            if pm_k is None:
+                pm = momentum_vectors(head_quantities, ks, core, kqm, latgen.Vol)
+                pm_k = pm.__getitem__
         r = chi0_eps(kcw, minm_k, nkp, self.matsize, nb1, nb2, nom, pm_k=pm_k, head=head, Ul=Ul, dUl=dUl)
         eps, epsw1, epsw2, head_out = r.numpy()
         if fout is not None:

@@ -16,9 +16,15 @@ reshape/product of the SVD branch.  The three Fortran kernels it calls
 with fr_convolution2) cannot be compiled here; they run from their Fortran
 text through ``f90py`` (beside this script), with the f2py calling
 convention the reference uses (outputs returned, sizes from the shapes), so
-the golden values are the reference's own statements end to end.  Output:
-``calc_selfc_golden.npz`` beside this script.
+the golden values are the reference's own statements end to end.
+
+Cases: a finite q; q = 0 with head and wings on a dense frequency mesh
+(iopfreq 4, the spline branch); a finite q in an SVD basis; and a finite q on
+the dense mesh with W Hermitian at each frequency (mwm real up to rounding,
+so the spline of its imaginary part is skipped) and no core states (no core
+block from calc_minm).  Output: ``calc_selfc_golden.npz`` beside this script.
 """
+import contextlib
 import io
 import itertools
 import math
@@ -101,10 +107,13 @@ def load(saved, enks):
     return refsrc.load(PYGW, "    def calc_selfc(self,", "    ", ns, "calc_selfc")
 
 
-def case(rng, iq, npb=16, nkp=4, ibgw=1, nbgw=3, ncg_c=1, nbands_c=6, nom=5, nl=None, dense=False):
+def case(rng, iq, npb=16, nkp=4, ibgw=1, nbgw=3, ncg_c=1, nbands_c=6, nom=5, nl=None, dense=False,
+         hermitian=False):
     nb1, nb2 = nbgw - ibgw, nbands_c
     nw = nom if nl is None else nl
     W = 0.3 * (rng.standard_normal((npb, npb, nw)) + 1j * rng.standard_normal((npb, npb, nw)))
+    if hermitian:            # W Hermitian at each frequency: mwm real up to rounding
+        W = 0.5 * (W + np.conj(W.transpose(1, 0, 2)))
     M = 0.2 * (rng.standard_normal((nkp, nb1, nb2, npb)) + 1j * rng.standard_normal((nkp, nb1, nb2, npb)))
     Ebnd = np.sort(rng.uniform(-1.0, 2.0, (1, nkp, nbands_c)), axis=2)
     core_e = [-8.0 - rng.uniform(0, 1)]
@@ -122,7 +131,8 @@ def case(rng, iq, npb=16, nkp=4, ibgw=1, nbgw=3, ncg_c=1, nbands_c=6, nom=5, nl=
     singc1, singc2, Vol = 0.7, 1.3, 250.0
 
     def calc_minm(ik, iq_, band_limits, kind, *a):
-        return M[ik][:, ncg_c:, :].copy(), M[ik][:, :ncg_c, :].copy()          # valence, core
+        # valence, core (None without core states, as calc_minm returns it)
+        return M[ik][:, ncg_c:, :].copy(), (M[ik][:, :ncg_c, :].copy() if ncg_c else None)
 
     me = NS(singc1=singc1, singc2=singc2, calc_minm=calc_minm)
     kqm = NS(qlistc=np.zeros((2, 3), dtype=int), LCMq=1, qlist=np.zeros((3, 3)), weight=np.ones(nkp),
@@ -151,11 +161,17 @@ def case(rng, iq, npb=16, nkp=4, ibgw=1, nbgw=3, ncg_c=1, nbands_c=6, nom=5, nl=
 def main():
     warnings.filterwarnings("ignore", category=SyntaxWarning)    # escape sequences in the reference's docstrings
     rng = np.random.default_rng(20261204)
-    cases = {
-        "q": case(rng, 1),
-        "q0dense": case(rng, 0, dense=True),
-        "svd": case(rng, 1, nl=3),
-    }
+    coverage = "--coverage" in sys.argv          # list the statements no case executes, store nothing
+    with (refsrc.Trace() if coverage else contextlib.nullcontext()) as trace:
+        cases = {
+            "q": case(rng, 1),
+            "q0dense": case(rng, 0, dense=True),
+            "svd": case(rng, 1, nl=3),
+            "densereal": case(rng, 1, ncg_c=0, dense=True, hermitian=True),
+        }
+    if coverage:
+        refsrc.report(trace)
+        return
     flat = {f"{c}.{k}": v for c, d in cases.items() for k, v in d.items()}
     np.savez_compressed(OUT, **flat)
     print(f"wrote {OUT}: " + ", ".join(f"{k}{tuple(np.shape(v))}" for k, v in flat.items()))

@@ -79,7 +79,52 @@ def extract(path, head, indent, replace=()):
     return textwrap.dedent("\n".join(py3_line(l, replace) for l in lines[start:end]))
 
 
+SOURCES = {}        # "path:name" -> source text of each function load() compiled
+
+
 def load(path, head, indent, namespace, name, replace=()):
     """Compile the extracted function into ``namespace`` and return it."""
-    exec(compile(extract(path, head, indent, replace), f"{path}:{name}", "exec"), namespace)
+    src = extract(path, head, indent, replace)
+    SOURCES[f"{path}:{name}"] = src
+    exec(compile(src, f"{path}:{name}", "exec"), namespace)
     return namespace[name]
+
+
+class Trace:
+    """Context manager recording which lines of the loaded functions run."""
+
+    def __init__(self):
+        self.hits = {}
+
+    def _global(self, frame, event, arg):
+        return self._local if frame.f_code.co_filename in SOURCES else None
+
+    def _local(self, frame, event, arg):
+        if event == "line":
+            self.hits.setdefault(frame.f_code.co_filename, set()).add(frame.f_lineno)
+        return self._local
+
+    def __enter__(self):
+        sys.settrace(self._global)
+        return self
+
+    def __exit__(self, *exc):
+        sys.settrace(None)
+        return False
+
+
+def report(trace):
+    """Print, per loaded function, how many of its statements ran and those
+    that never did."""
+    for fn, src in SOURCES.items():
+        lines, stack = set(), [compile(src, fn, "exec")]
+        while stack:
+            c = stack.pop()
+            lines.update(ln for _, _, ln in c.co_lines() if ln)
+            stack.extend(x for x in c.co_consts if hasattr(x, "co_lines"))
+        text = src.split("\n")
+        lines = {ln for ln in lines if not text[ln - 1].lstrip().startswith("def ")}
+        miss = sorted(lines - trace.hits.get(fn, set()))
+        print(f"{fn}: {len(lines) - len(miss)}/{len(lines)} statements executed")
+        for ln in miss:
+            print("    never:", text[ln - 1].strip())

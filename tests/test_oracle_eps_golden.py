@@ -1,7 +1,7 @@
 """The numpy oracle of calc_eps against golden vectors from the reference's own
 calc_eps (pygw.py:3039-3297), run on seeded inputs by
 tests/golden/make_calc_eps_golden.py: a finite q, q = 0 with head and wings,
-and q = 0 in an SVD frequency basis.  Both sides are FP64 numpy; only the
+q = 0 in an SVD frequency basis, and q = 0 with core states.  Both sides are FP64 numpy; only the
 order of some sums differs, so the bar is 1e-12 of the largest entry.  The
 GPU paths are checked against this oracle (tests/test_gpu_*.py)."""
 import os
@@ -22,7 +22,7 @@ def _close(got, ref, tol=1e-12):
     return np.abs(np.asarray(got) - ref).max() <= tol * max(np.abs(ref).max(), 1e-300)
 
 
-@pytest.mark.parametrize("case", ["q", "q0", "q0svd"])
+@pytest.mark.parametrize("case", ["q", "q0", "q0svd", "q0core"])
 def test_oracle_calc_eps_matches_the_reference_code(case):
     M, kcw = _g(case, "M"), _g(case, "kcw")
     npb = M.shape[-1]
@@ -39,3 +39,29 @@ def test_oracle_calc_eps_matches_the_reference_code(case):
         assert _close(w1, _g(case, "epsw1"))
         assert _close(w2, _g(case, "epsw2"))
         assert _close(head, _g(case, "head"))
+
+
+@pytest.mark.parametrize("case", ["q0", "q0svd", "q0core"])
+def test_product_momentum_vectors_match_the_reference_code(case):
+    """The product's host-side q→0 vectors (eps.momentum_vectors), formed from
+    the reference's head_quantities (momentum elements stored from band mst,
+    core levels first; pygw.py:3089-3093, 3120-3141), equal the vectors the
+    oracle above reproduces the reference's wings with, bit for bit."""
+    from types import SimpleNamespace as NS
+
+    from pygw_gb300 import eps as peps
+    g = lambda k: _g(case, k)  # noqa: E731
+    nkp = g("M").shape[0]
+    ecore = g("ecore")
+    ncg = len(ecore)
+    nvbm1, ncbm = (int(x) for x in g("nomax_numin"))
+    Ebnd = g("Ebnd")
+    ks = NS(nomax_numin=(nvbm1, ncbm), ncg_p=ncg, nbmaxpol=Ebnd.shape[2], Ebnd=Ebnd)
+    core = NS(corind=np.array([[0, 0, ic] for ic in range(ncg)], dtype=int).reshape(ncg, 3),
+              eig_core=[[list(ecore)]])
+    kqm = NS(kii_ind=np.arange(nkp))
+    hq = (g("head_in"), g("mmatcv"), g("mmatvv"), int(g("mst")))
+    pm = peps.momentum_vectors(hq, ks, core, kqm, float(g("Vol")))
+    assert pm.shape == g("pm").shape
+    assert np.array_equal(pm, g("pm"))
+    assert np.count_nonzero(pm) == pm.size
