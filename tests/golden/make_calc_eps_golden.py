@@ -23,7 +23,6 @@ core states (calc_minm's core block ``minc0`` ahead of the valence one, core
 levels from ``core.eig_core``, core-to-empty momentum elements ``mmatcv``)
 and momentum elements stored from band ``mst`` = 1 on.
 """
-import contextlib
 import io
 import itertools
 import os
@@ -121,21 +120,16 @@ def case(rng, iq, nkp, nvbm, ncbm, nb2, npb, nom, nl=None, ncg=0, mst=0):
 
 def main():
     rng = np.random.default_rng(20261203)
-    coverage = "--coverage" in sys.argv          # list the statements no case executes, store nothing
-    with (refsrc.Trace() if coverage else contextlib.nullcontext()) as trace:
-        cases = {
-            "q": case(rng, 1, nkp=6, nvbm=3, ncbm=3, nb2=5, npb=24, nom=4),
-            "q0": case(rng, 0, nkp=6, nvbm=3, ncbm=3, nb2=5, npb=24, nom=4),
-            "q0svd": case(rng, 0, nkp=6, nvbm=3, ncbm=3, nb2=5, npb=24, nom=6, nl=4),
-            "q0core": case(rng, 0, nkp=6, nvbm=3, ncbm=3, nb2=5, npb=24, nom=4, ncg=2, mst=1),
-        }
-    if coverage:
-        refsrc.report(trace)
-        return
+    cases = {
+        "q": case(rng, 1, nkp=6, nvbm=3, ncbm=3, nb2=5, npb=24, nom=4),
+        "q0": case(rng, 0, nkp=6, nvbm=3, ncbm=3, nb2=5, npb=24, nom=4),
+        "q0svd": case(rng, 0, nkp=6, nvbm=3, ncbm=3, nb2=5, npb=24, nom=6, nl=4),
+        "q0core": case(rng, 0, nkp=6, nvbm=3, ncbm=3, nb2=5, npb=24, nom=4, ncg=2, mst=1),
+    }
     flat = {f"{c}.{k}": np.asarray(v) for c, d in cases.items() for k, v in d.items()}
     np.savez_compressed(OUT, **flat)
     print(f"wrote {OUT}: " + ", ".join(f"{k}{tuple(v.shape)}" for k, v in flat.items()))
 
 
 if __name__ == "__main__":
-    main()
+    refsrc.run(main)

@@ -24,7 +24,6 @@ the dense mesh with W Hermitian at each frequency (mwm real up to rounding,
 so the spline of its imaginary part is skipped) and no core states (no core
 block from calc_minm).  Output: ``calc_selfc_golden.npz`` beside this script.
 """
-import contextlib
 import io
 import itertools
 import math
@@ -161,21 +160,16 @@ def case(rng, iq, npb=16, nkp=4, ibgw=1, nbgw=3, ncg_c=1, nbands_c=6, nom=5, nl=
 def main():
     warnings.filterwarnings("ignore", category=SyntaxWarning)    # escape sequences in the reference's docstrings
     rng = np.random.default_rng(20261204)
-    coverage = "--coverage" in sys.argv          # list the statements no case executes, store nothing
-    with (refsrc.Trace() if coverage else contextlib.nullcontext()) as trace:
-        cases = {
-            "q": case(rng, 1),
-            "q0dense": case(rng, 0, dense=True),
-            "svd": case(rng, 1, nl=3),
-            "densereal": case(rng, 1, ncg_c=0, dense=True, hermitian=True),
-        }
-    if coverage:
-        refsrc.report(trace)
-        return
+    cases = {
+        "q": case(rng, 1),
+        "q0dense": case(rng, 0, dense=True),
+        "svd": case(rng, 1, nl=3),
+        "densereal": case(rng, 1, ncg_c=0, dense=True, hermitian=True),
+    }
     flat = {f"{c}.{k}": v for c, d in cases.items() for k, v in d.items()}
     np.savez_compressed(OUT, **flat)
     print(f"wrote {OUT}: " + ", ".join(f"{k}{tuple(np.shape(v))}" for k, v in flat.items()))
 
 
 if __name__ == "__main__":
-    main()
+    refsrc.run(main)

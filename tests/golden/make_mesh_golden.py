@@ -122,4 +122,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    refsrc.run(main)

@@ -22,6 +22,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
+import refsrc  # noqa: E402
 from refsrc import NS, load, reference_file  # noqa: E402
 
 PYGW = reference_file("pygw.py")
@@ -70,4 +71,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    refsrc.run(main)

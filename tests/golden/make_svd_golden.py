@@ -5,7 +5,8 @@ Run where the reference's source tree is available:
     python tests/golden/make_svd_golden.py --reference <PyGW source tree>
 
 Runs the text of ``svd_functions`` (pygw.py:3478-3501) and of
-``Give2TanMesh`` (mcommon.py:13-31) on two Matsubara meshes.  Two Python 2
+``Give2TanMesh`` (mcommon.py:13-31) on three Matsubara meshes, the third with a
+lower frequency bound that Give2TanMesh clamps.  Two Python 2
 forms are rewritten: print statements become print() calls, and the integer
 division ``len(iom)/2`` becomes ``len(iom)//2`` (what it computes under
 Python 2).  The reference's ``linalg`` there is scipy.linalg.  Output:
@@ -45,7 +46,9 @@ def main():
     out = {}
     for name, (nom, om_min, om_max, om_nom, cut) in {
             "a": (32, 1e-3, 20.0, 60, 1e-10),
-            "b": (48, 5e-4, 40.0, 80, 1e-8)}.items():
+            "b": (48, 5e-4, 40.0, 80, 1e-8),
+            # om_min above L * Nw * tan(pi / 2Nw)^2 / 4: Give2TanMesh clamps it
+            "c": (24, 0.1, 1.0, 10, 1e-8)}.items():
         x = np.polynomial.legendre.leggauss(nom)
         t = 0.5 * (x[0] + 1.0)
         iomega = 0.02 * t / (1.0 - t + 1e-3)                   # a Matsubara-like mesh, dense near 0
@@ -60,4 +63,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    refsrc.run(main)

@@ -1,6 +1,7 @@
 """The SVD frequency basis of the product (pygw_gb300.svd) against golden
 vectors from the reference's own svd_functions (pygw.py:3478-3501) and
-Give2TanMesh (mcommon.py:13-31), run on two Matsubara meshes by
+Give2TanMesh (mcommon.py:13-31), run on three Matsubara meshes (one with a
+lower bound that Give2TanMesh clamps) by
 tests/golden/make_svd_golden.py.  Both use scipy's SVD; a singular vector is
 compared up to its sign."""
 import os
@@ -13,7 +14,7 @@ from pygw_gb300 import svd
 GOLDEN = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "svd_golden.npz"))
 
 
-@pytest.mark.parametrize("case", ["a", "b"])
+@pytest.mark.parametrize("case", ["a", "b", "c"])
 def test_svd_basis_matches_the_reference_code(case):
     g = lambda k: GOLDEN[f"{case}.{k}"]  # noqa: E731
     om_min, om_max, om_nom, cut = g("args")
