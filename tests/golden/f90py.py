@@ -1393,6 +1393,9 @@ def unexecuted(tr, hits):
     return out
 
 
+LOADED = []            # every Translator load() made, for coverage reports
+
+
 def load(paths, names, atan, log):
     """Translate the procedures ``names`` (and whatever they call, on demand)
     from the Fortran files ``paths``; returns {name: callable}."""
@@ -1401,6 +1404,7 @@ def load(paths, names, atan, log):
         with open(path) as f:
             units.update(parse_units(f.read()))
     tr = Translator(units, atan, log)
+    LOADED.append(tr)
     tr.ns["_frange"] = _frange
     tr.ns["_proc"] = lambda nm: tr.procedure(nm)
     return {n: tr.procedure(n) for n in names}, tr

@@ -37,7 +37,8 @@ Output: ``weights_golden.npz`` (inputs and the reference's ``kcw`` of par2
 and par3 for each math variant); nothing of the reference's source is
 stored.  ``--check-c1`` instead compares the oracle (with the reference's
 layout of 7- and 8-node halves) with the reference's statements on the full
-C1 problem and stores nothing.
+C1 problem and stores nothing; ``--coverage`` lists the statements of the
+translated routines that no case executes and stores nothing.
 """
 import math
 import os
@@ -51,6 +52,7 @@ sys.path.insert(0, HERE)
 sys.path.insert(0, ROOT)
 import f90py  # noqa: E402
 f90py.POISON = True     # a read of storage never written shows as NaN, or raises
+import refsrc  # noqa: E402
 from refsrc import reference_file  # noqa: E402
 
 OUT = os.path.join(HERE, "weights_golden.npz")
@@ -213,4 +215,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    refsrc.run(main)

@@ -91,13 +91,15 @@ def load(path, head, indent, namespace, name, replace=()):
 
 
 class Trace:
-    """Context manager recording which lines of the loaded functions run."""
+    """Context manager recording which lines of the loaded functions (and of
+    Fortran procedures translated by f90py) run."""
 
     def __init__(self):
         self.hits = {}
 
     def _global(self, frame, event, arg):
-        return self._local if frame.f_code.co_filename in SOURCES else None
+        fn = frame.f_code.co_filename
+        return self._local if fn in SOURCES or fn.startswith("<f90:") else None
 
     def _local(self, frame, event, arg):
         if event == "line":
@@ -128,6 +130,17 @@ def report(trace):
         print(f"{fn}: {len(lines) - len(miss)}/{len(lines)} statements executed")
         for ln in miss:
             print("    never:", text[ln - 1].strip())
+    f90py = sys.modules.get("f90py")
+    hits = {fn[5:-1]: ls for fn, ls in trace.hits.items() if fn.startswith("<f90:")}
+    done = set()
+    for tr in (f90py.LOADED if f90py else []):      # each translated procedure once
+        for unit, (n_run, n_all, miss) in f90py.unexecuted(tr, hits).items():
+            if unit in done:
+                continue
+            done.add(unit)
+            print(f"Fortran {unit}: {n_run}/{n_all} statements executed")
+            for m in miss:
+                print("    never:", m)
 
 
 def run(main):

@@ -65,3 +65,40 @@ def test_product_momentum_vectors_match_the_reference_code(case):
     assert pm.shape == g("pm").shape
     assert np.array_equal(pm, g("pm"))
     assert np.count_nonzero(pm) == pm.size
+
+
+def test_drop_in_calc_eps_forms_the_q0_vectors_from_head_quantities(monkeypatch):
+    """MatrixElements2Band.calc_eps at q = 0 with the reference's arguments
+    hands the contraction the reference's q→0 vectors and head (the GPU call
+    itself is replaced by a recorder here)."""
+    from types import SimpleNamespace as NS
+
+    from pygw_gb300 import eps as peps
+    case = "q0core"
+    g = lambda k: _g(case, k)  # noqa: E731
+    M, kcw = g("M"), g("kcw")
+    nkp, nb1, nb2, npb = M.shape
+    ecore = g("ecore")
+    ncg = len(ecore)
+    seen = {}
+
+    def recorder(kcw_, minm, nkp_, npb_, nb1_, nb2_, nom_, pm_k=None, head=None, Ul=None, dUl=None):
+        seen.update(pm=np.stack([pm_k(ik) for ik in range(nkp_)]), head=head, shape=(nkp_, npb_, nb1_, nb2_, nom_),
+                    minm=np.stack([minm(ik) for ik in range(nkp_)]))
+        z = np.zeros((npb_, npb_, nom_), complex)
+        return NS(numpy=lambda: (z, None, None, None))
+
+    monkeypatch.setattr(peps, "chi0_eps", recorder)
+    nvbm1, ncbm = (int(x) for x in g("nomax_numin"))
+    Ebnd = g("Ebnd")
+    ks = NS(nomax_numin=(nvbm1, ncbm), ncg_p=ncg, nbmaxpol=Ebnd.shape[2], Ebnd=Ebnd)
+    core = NS(corind=np.array([[0, 0, ic] for ic in range(ncg)], dtype=int).reshape(ncg, 3),
+              eig_core=[[list(ecore)]])
+    kqm = NS(kii_ind=np.arange(nkp))
+    me = peps.MatrixElements2Band(lambda ik, iq, bl, mode: (M[ik][ncg:], M[ik][:ncg]), npb)
+    hq = (g("head_in"), g("mmatcv"), g("mmatvv"), int(g("mst")))
+    me.calc_eps(0, hq, None, None, NS(Vol=float(g("Vol"))), kqm, ks, None, None, None, core, None,
+                NS(omega=np.zeros(kcw.shape[3])), kcw, "", None, None, None)
+    assert seen["shape"] == (nkp, npb, nb1, nb2, kcw.shape[3])
+    assert np.array_equal(seen["pm"], g("pm")) and np.array_equal(seen["head"], g("head_in"))
+    assert np.array_equal(seen["minm"], M)            # core block first, as calc_eps concatenates
