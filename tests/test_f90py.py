@@ -242,3 +242,25 @@ end subroutine pick
         procs["pick"](i4(3), r)
     ran, total, never = f90py.unexecuted(tr, t.hits)["pick"]
     assert r[()] == 1 and ran == total - 1 and len(never) == 1 and "-" in never[0]
+
+
+def test_subscripts_beyond_the_storage_raise_undefined(tmp_path):
+    """Out-of-bounds subscripts address the actual's storage as compiled code
+    without bounds checks does; beyond that storage the result is undefined
+    and the translator raises."""
+    src = """
+subroutine peek(w, n, i, x)
+  implicit none
+  integer, intent(in) :: n, i
+  real(8), intent(in) :: w(2, n)
+  real(8), intent(out) :: x
+  x = w(1, i)
+end subroutine peek
+"""
+    f = _load(src, ["peek"], tmp_path)["peek"]
+    w = FA(np.asfortranarray(np.arange(8.0).reshape(2, 4, order="F")), (1, 1))
+    x = np.array(0.0)
+    f(w, i4(2), i4(4), x)                   # outside the dummy's (2, 2), inside the actual's storage
+    assert x[()] == 6.0
+    with pytest.raises(f90py.Undefined):
+        f(w, i4(2), i4(5), x)
