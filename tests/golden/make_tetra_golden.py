@@ -32,12 +32,14 @@ share.  Each tetrahedron is classified:
   integer, or give weights that depend on a variable never written (run with
   ``f90py.POISON``: such reads give NaN or the integer type's lowest value):
   each undefined in compiled code;
-* 2 — they call ``stop``.
+* 2 — they call ``stop`` (also with ``POISON`` off: a stop reached only
+  from poisoned values follows from storage never written and is class 1);
+  ``stop_site`` records which one (``STOP_SITES``).
 
 ``--coverage`` stores nothing and instead lists, per translated routine, the
 statements that no well-defined tetrahedron executes.
 
-Output: ``tetra_golden.npz`` (e, f, omega, kind and weight per
+Output: ``tetra_golden.npz`` (e, f, omega, kind, stop_site and weight per
 tetrahedron); nothing of the reference's source is stored.
 """
 import contextlib
@@ -57,6 +59,9 @@ OUT = os.path.join(HERE, "tetra_golden.npz")
 FILES = ["for_tetrahedra.f90", "for_tetrahedra2.f90", "for_tetrahedra3.f90"]
 OMEGA = np.array([0.0, 1e-7, 1e-3, 0.05, 0.5, 5.0])
 COUNTS = {"grid": 400, "near": 300, "cont": 200, "equal": 200}
+# the stop messages of convw1t_par and its callees, by site code 1..
+STOP_SITES = ["ERROR in sortnodes", "error in sortnodes, nnod=6", "error in setnodes", "ERROR in sorteq",
+              "ERROR in convw1t", "ERROR in stweight_imat"]
 
 
 def corner_sets(kind, n, rng):
@@ -96,27 +101,46 @@ def main():
     conv = procs["convw1t_par"]
     nom = len(OMEGA)
     rng = np.random.default_rng(7)
-    E, F, K, W = [], [], [], []
+    def call(e, f):
+        w = f90py.FArr(np.zeros((4, nom), order="F"), (1, 1))
+        conv(w, f90py.FArr(e.copy(), (1,)), f90py.FArr(f.copy(), (1,)), np.array(0.0),
+             f90py.FArr(OMEGA.copy(), (1,)), np.array(nom, dtype=np.int32), np.array(False))
+        return w
+
+    def stop_site(ex):
+        msg = str(ex).strip("'\" ")
+        return STOP_SITES.index(msg) + 1
+
+    E, F, K, S, W = [], [], [], [], []
     hits = {}
     for kind, n in COUNTS.items():
         for e, f in corner_sets(kind, n, rng):
-            w = f90py.FArr(np.zeros((4, nom), order="F"), (1, 1))
             trace = f90py.LineTrace() if coverage else contextlib.nullcontext()
+            site = 0
             try:
                 with trace:
-                    conv(w, f90py.FArr(e.copy(), (1,)), f90py.FArr(f.copy(), (1,)), np.array(0.0),
-                         f90py.FArr(OMEGA.copy(), (1,)), np.array(nom, dtype=np.int32), np.array(False))
+                    w = call(e, f)
                 k = 0 if np.isfinite(w.a).all() else 1
             except f90py.Undefined:
                 k = 1
             except f90py.FortranStop:
-                k = 2
+                f90py.POISON = False              # does it stop from defined values too?
+                try:
+                    call(e, f)
+                    k = 1
+                except f90py.Undefined:
+                    k = 1
+                except f90py.FortranStop as ex:
+                    k, site = 2, stop_site(ex)
+                finally:
+                    f90py.POISON = True
             if coverage and k == 0:
                 for u, ls in trace.hits.items():
                     hits.setdefault(u, set()).update(ls)
             E.append(e)
             F.append(f)
             K.append(k)
+            S.append(site)
             W.append(w.a.copy() if k == 0 else np.zeros((4, nom)))
         print(kind, n, "done", flush=True)
     if coverage:
@@ -127,7 +151,8 @@ def main():
                 print("    never:", m)
         return
     K = np.array(K, dtype=np.int8)
-    np.savez_compressed(OUT, e=np.array(E), f=np.array(F), omega=OMEGA, kind=K, weight=np.array(W))
+    np.savez_compressed(OUT, e=np.array(E), f=np.array(F), omega=OMEGA, kind=K, weight=np.array(W),
+                        stop_site=np.array(S, dtype=np.int8))
     print("wrote", OUT, "kinds:", np.bincount(K, minlength=3).tolist())
 
 
