@@ -37,7 +37,11 @@ share.  Each tetrahedron is classified:
   ``stop_site`` records which one (``STOP_SITES``).
 
 ``--coverage`` stores nothing and instead lists, per translated routine, the
-statements that no well-defined tetrahedron executes.
+statements that no well-defined tetrahedron executes.  ``--search SEED
+PER_KIND`` stores nothing and instead runs PER_KIND fresh corner sets of each
+kind from SEED through the statements and through the oracle (with the
+reference's layout of 7- and 8-node halves) and counts the sets where they
+disagree: different weights, or a status that does not match the class.
 
 Output: ``tetra_golden.npz`` (e, f, omega, kind, stop_site and weight per
 tetrahedron); nothing of the reference's source is stored.
@@ -96,11 +100,17 @@ def main():
         return float(ow.portable_math(np.array([x]))[1][0])
 
     coverage = "--coverage" in sys.argv
+    search = sys.argv.index("--search") if "--search" in sys.argv else None
+    counts, seed = COUNTS, 7
+    if search is not None:           # --search SEED PER_KIND: compare with the oracle, store nothing
+        seed, per = int(sys.argv[search + 1]), int(sys.argv[search + 2])
+        counts = {kind: per for kind in COUNTS}
     f90py.POISON = True
     procs, tr = f90py.load([reference_file(f) for f in FILES], ["convw1t_par"], portable_atan, portable_log)
     conv = procs["convw1t_par"]
     nom = len(OMEGA)
-    rng = np.random.default_rng(7)
+    rng = np.random.default_rng(seed)
+
     def call(e, f):
         w = f90py.FArr(np.zeros((4, nom), order="F"), (1, 1))
         conv(w, f90py.FArr(e.copy(), (1,)), f90py.FArr(f.copy(), (1,)), np.array(0.0),
@@ -113,7 +123,7 @@ def main():
 
     E, F, K, S, W = [], [], [], [], []
     hits = {}
-    for kind, n in COUNTS.items():
+    for kind, n in counts.items():
         for e, f in corner_sets(kind, n, rng):
             trace = f90py.LineTrace() if coverage else contextlib.nullcontext()
             site = 0
@@ -143,6 +153,16 @@ def main():
             S.append(site)
             W.append(w.a.copy() if k == 0 else np.zeros((4, nom)))
         print(kind, n, "done", flush=True)
+    if search is not None:
+        bad = 0
+        with ow.reference_layout():
+            for e, f, k, site, w in zip(E, F, K, S, W):
+                got, st, _ = ow.convw1t(e, f, 0.0, OMEGA)
+                bad += bool((k == 0 and (st or not np.array_equal(got, w))) or (k == 1 and not st & 32)
+                            or (k == 2 and (not st or st & 32)))
+        print(f"{len(K)} corner sets (seed {seed}): {np.bincount(K, minlength=3).tolist()} defined / undefined / "
+              f"stop; {bad} where the oracle disagrees")
+        return
     if coverage:
         # statements the well-defined tetrahedra never execute
         for u, (n_run, n_all, miss) in f90py.unexecuted(tr, hits).items():

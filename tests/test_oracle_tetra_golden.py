@@ -98,3 +98,31 @@ def test_static_limit_branches_are_present(golden):
     w = g["weight"][ok]
     assert g["omega"][0] == 0.0 and np.isfinite(w).all()
     assert np.count_nonzero(w[:, :, 0]) > 100
+
+
+def test_well_defined_tetrahedra_through_the_mesh_driver(golden):
+    """The same corner sets embedded in a mesh and run through the oracle's
+    bz_calcqdepw_par2 (for_tetrahedra.f90:390-464): one tetrahedron per four
+    k-points with the occupied band as band 0 and the empty one as band 1,
+    k − q = k, and filler tetrahedra (ntet = 6·nkp, as the driver's tetln
+    requires) on four extra k-points where both bands lie below EF, so that
+    every filler item is skipped.  Each k-point then holds one corner's
+    weight times 6·wtet, formed as the driver forms it: (w·6)·(1/ntet)."""
+    g = golden
+    ok = np.flatnonzero(g["kind"] == 0)
+    n = len(ok)
+    nkp = 4 * n + 4
+    ntet = 6 * nkp
+    enk = np.full((2, nkp), -1.0)
+    enk[0, :4 * n] = g["e"][ok].ravel()
+    enk[1, :4 * n] = g["f"][ok].ravel()
+    tetc = np.full((4, ntet), 4 * n, dtype=np.int32) + np.arange(4, dtype=np.int32)[:, None]
+    tetc[:, :n] = 4 * np.arange(n)[None, :] + np.arange(4)[:, None]
+    om = g["omega"]
+    with ow.reference_layout():
+        kcw, st, _ = ow.bz_calcqdepw_par2(np.asfortranarray(enk), 0.0, np.arange(nkp), 0, 0, 1, om,
+                                          np.asfortranarray(tetc), return_stats=True)
+    want = np.zeros((nkp, len(om)))
+    want[:4 * n] = ((g["weight"][ok] * 6.0) * (1.0 / ntet)).reshape(4 * n, len(om))
+    assert st == 0 and kcw.shape == (1, 1, nkp, len(om))
+    assert np.array_equal(kcw[0, 0], want)
