@@ -988,7 +988,10 @@ static void convw1t(double* weight, const double e[4], const double f[4], double
         // the reference's addressing of wtemp(4,2,nom) as (4,nom,2): the first
         // half's weights survive for the first two frequencies only
         // (element (c, j) of the Fortran (4, nom) array lies 4·j + c values in;
-        // this restatement stores it at c·nom + j)
+        // this restatement stores it at c·nom + j).  With one frequency the
+        // second half starts 8 values into an 8-value wtemp, past its end:
+        // undefined, and the halves are added as an undisturbed stack would.
+        if (nom < 2) st.status |= ERR_UNDEFINED;
         for (int c = 0; c < 4; c++)
           for (int j = 0; j < nom; j++)
             weight[c * nom + j] = (j < 2 ? w1[c * nom + j] : w2[c * nom + j - 2]) + w2[c * nom + j];

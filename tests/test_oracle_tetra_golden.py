@@ -126,3 +126,22 @@ def test_well_defined_tetrahedra_through_the_mesh_driver(golden):
     want[:4 * n] = ((g["weight"][ok] * 6.0) * (1.0 / ntet)).reshape(4 * n, len(om))
     assert st == 0 and kcw.shape == (1, 1, nkp, len(om))
     assert np.array_equal(kcw[0, 0], want)
+
+
+def test_one_frequency_seven_and_eight_node_halves_are_undefined_in_the_reference_layout(golden):
+    """convw1t_par's wtemp(4,2,nom) holds 8·nom values and the second half of
+    a 7- or 8-node polyhedron is written from the 9th on (for_tetrahedra3.f90:
+    36, 100-120): with one frequency that lies past the array's end, which is
+    undefined in compiled code; the oracle then flags it (reference layout
+    only) and adds the halves.  With two frequencies it is defined."""
+    g = golden
+    big = [i for i in np.flatnonzero(g["kind"] == 0) if _run(g, i)[2] >= 7][:20]
+    assert big
+    for i in big:
+        for nom, flagged in ((1, True), (2, False)):
+            om = g["omega"][3:3 + nom]
+            with ow.reference_layout():
+                w, st, _ = ow.convw1t(g["e"][i], g["f"][i], 0.0, om)
+            w0, st0, _ = ow.convw1t(g["e"][i], g["f"][i], 0.0, om)
+            assert bool(st & ERR_UNDEFINED) == flagged and st0 == 0
+            assert np.array_equal(w, w0)
