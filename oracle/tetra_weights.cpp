@@ -7,7 +7,12 @@
 // kept) on seeded inputs; this restatement reproduces those kcw bit for bit
 // with either atan/log (tests/test_oracle_weights_golden.py), except where the
 // reference's wtemp(4,2,nom) layout aliases the halves of 7- and 8-node
-// polyhedra from the third frequency on (see convw1t below).  Known answers
+// polyhedra from the third frequency on (see convw1t below).  Per tetrahedron,
+// tests/golden/make_tetra_golden.py runs convw1t_par on seeded corner sets
+// that reach every statement of these routines outside error exits, debug
+// output, one dead branch and one undefined case; this restatement matches
+// each well-defined set bit for bit and flags each undefined or stopping one
+// (tests/test_oracle_tetra_golden.py).  Known answers
 // (tests/test_oracle_weights.py) check the integrals themselves.
 //
 // CPU restatement of PyGW's imaginary-axis tetrahedron polarization weights
