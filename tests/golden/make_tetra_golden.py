@@ -25,7 +25,8 @@ reaches the geometric cases far more densely than band structures on a mesh:
   tolerance of 1e-2, including chains that are not transitive).
 
 atan and log are the portable implementations the oracle and the GPU kernels
-share.  Each tetrahedron is classified:
+share; the well-defined sets are run once more with the C library's atan and
+log (``weight_libm``).  Each tetrahedron is classified:
 
 * 0 — the reference's statements run to the end; ``weight[4, nom]`` stored;
 * 1 — they address outside an array's storage, test a bit outside an
@@ -43,10 +44,11 @@ kind from SEED through the statements and through the oracle (with the
 reference's layout of 7- and 8-node halves) and counts the sets where they
 disagree: different weights, or a status that does not match the class.
 
-Output: ``tetra_golden.npz`` (e, f, omega, kind, stop_site and weight per
-tetrahedron); nothing of the reference's source is stored.
+Output: ``tetra_golden.npz`` (e, f, omega, kind, stop_site, weight and
+weight_libm per tetrahedron); nothing of the reference's source is stored.
 """
 import contextlib
+import math
 import os
 import sys
 
@@ -171,8 +173,15 @@ def main():
                 print("    never:", m)
         return
     K = np.array(K, dtype=np.int8)
+    # the well-defined sets once more with the C library's atan/log
+    procs_libm, _ = f90py.load([reference_file(f) for f in FILES], ["convw1t_par"], math.atan, math.log)
+    conv = procs_libm["convw1t_par"]
+    WL = np.zeros((len(K), 4, nom))
+    for i in np.flatnonzero(K == 0):
+        WL[i] = call(E[i], F[i]).a
+        assert np.isfinite(WL[i]).all()
     np.savez_compressed(OUT, e=np.array(E), f=np.array(F), omega=OMEGA, kind=K, weight=np.array(W),
-                        stop_site=np.array(S, dtype=np.int8))
+                        weight_libm=WL, stop_site=np.array(S, dtype=np.int8))
     print("wrote", OUT, "kinds:", np.bincount(K, minlength=3).tolist())
 
 

@@ -50,6 +50,16 @@ def test_well_defined_tetrahedra_match_bit_for_bit(golden):
     assert all(counts[n] > 0 for n in range(3, 9)), counts
 
 
+def test_well_defined_tetrahedra_match_with_the_c_library_atan_log(golden):
+    """The same statements with the C library's atan/log (what a compiled
+    reference calls) against the oracle built with them: bit for bit too."""
+    g = golden
+    with ow.reference_layout():
+        for i in np.flatnonzero(g["kind"] == 0):
+            w, st, _ = ow.convw1t(g["e"][i], g["f"][i], 0.0, g["omega"], libm=True)
+            assert st == 0 and np.array_equal(w, g["weight_libm"][i]), i
+
+
 def test_default_layout_differs_only_where_the_halves_alias(golden):
     """Without the reference's layout the oracle adds the two halves of a
     7- or 8-node polyhedron at every frequency; it then differs from the
